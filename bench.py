@@ -1,0 +1,353 @@
+"""Throughput of PNFFT's trafo+adj on one GB300 (and the CPU oracle beside it).
+
+Workload (the configuration the headline metric is quoted on): c2c 3-D NFFT,
+N = 128^3 Fourier coefficients, oversampled grid n = 256^3, M = 2^22 nodes
+i.i.d. uniform in [-0.5,0.5)^3, Kaiser-Bessel window m = 6, f_hat complex
+normal scaled by (1+|k|^2)^-1, adj input f complex normal (seeded synthetic
+data).  One step = pnfft_trafo (D, F, B) + pnfft_adj (B^T, F^H, D^T).
+
+  value   Mpts/s = M / (t_trafo + t_adj), FP32-mixed, inputs resident in HBM
+          (zero-copy device entry points), nodes re-binned every call
+  e2e     same metric through the C ABI (pnfft_trafo/pnfft_adj) on host
+          arrays from pnfft_malloc (page-locked): copies inside the timed step
+  fp64    the plain FP64 path, same workload
+Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CFG = dict(N=(128, 128, 128), n=(256, 256, 256), M=1 << 22, m=6)
+WORKLOAD = "c2c NFFT trafo+adj, N=128^3, n=256^3, M=2^22 uniform nodes, Kaiser-Bessel m=6"
+METRIC = "trafo+adj Mpts/s, N=128^3 M=2^22"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def make_inputs(seed=2):
+    N, M = CFG["N"], CFG["M"]
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    k = [np.arange(-n // 2, n // 2) for n in N]
+    K0, K1, K2 = np.meshgrid(*k, indexing="ij")
+    w = 1.0 / (1.0 + K0 ** 2 + K1 ** 2 + K2 ** 2)
+    fh = ((rng.standard_normal(N) + 1j * rng.standard_normal(N)) * w).ravel()
+    f = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    return x, fh, f
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+            dev = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0] or "0"
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={dev}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            c = [v.strip() for v in line.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                smax.append(float(c[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, c[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(nthreads=0, m_sample=1 << 15):
+    """Oracle (CPU port of the reference) on a bounded sample of the workload:
+    D/F/F^H/D^T on the full N=128^3 / n=256^3 grid and B/B^T on m_sample of
+    the nodes; the node-proportional part is scaled to M (M/m_sample)."""
+    from oracle import pnfft_oracle as O
+    x, fh, f = make_inputs()
+    N, n, M, m = CFG["N"], CFG["n"], CFG["M"], CFG["m"]
+    p = O.OraclePlan(N, n, m=m, flags=0, nthreads=nthreads)
+    xs, fs = x[:m_sample].copy(), f[:m_sample].copy()
+    t0 = time.perf_counter()
+    g1 = p.trafo_D(fh, 0)
+    grid = p.forward_F(g1)
+    t1 = time.perf_counter()
+    out = np.zeros(m_sample, complex)
+    p.trafo_B(xs, grid, f=out.view(np.float64), cflags=O.COMPUTE_F)
+    t2 = time.perf_counter()
+    g = p.adjoint_B(xs, f=fs.view(np.float64), cflags=O.COMPUTE_F)
+    t3 = time.perf_counter()
+    gh = p.adjoint_F(g)
+    acc = np.zeros(int(np.prod(p.local_N)), complex)
+    p.adjoint_D(gh, 0, acc)
+    t4 = time.perf_counter()
+    fixed = (t1 - t0) + (t4 - t3)
+    per_node = ((t2 - t1) + (t3 - t2)) / m_sample
+    t_full = fixed + per_node * M
+    cores = nthreads if nthreads > 0 else O.num_threads()
+    return {"value": M / t_full / 1e6, "unit": "Mpts/s", "cores": cores, "kind": "port",
+            "sample": f"oracle FP64: D+F+F^H+D^T on the full 256^3 grid ({fixed:.2f} s) + B and B^T on "
+                      f"{m_sample} of the 2^22 nodes ({(t3 - t1):.2f} s), node part scaled by {M // m_sample}",
+            "seconds_per_step_extrapolated": t_full}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    for _ in range(args.warmup):
+        cpu_sample()
+    vals, secs = [], []
+    for _ in range(args.steps):
+        r = cpu_sample()
+        vals.append(r["value"])
+        secs.append(r["seconds_per_step_extrapolated"])
+    v = statistics.median(vals)
+    line = {"metric": METRIC, "value": v, "unit": "Mpts/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "precision": "fp64", "l2": "n/a (CPU)"}, "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "Mpts/s", "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": v, "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    import pnfft_gb300 as P
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    N, n, M, m = CFG["N"], CFG["n"], CFG["M"], CFG["m"]
+    x, fh, f = make_inputs(seed=2 + rank)
+    dev = torch.device("cuda", local)
+    xd = torch.tensor(x, device=dev)
+    fhd = torch.tensor(fh, device=dev)
+    fd = torch.tensor(f, device=dev)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def device_steps(plan, K, W, fixed=False):
+        out_f = torch.empty(M, dtype=torch.complex128, device=dev)
+        out_fh = torch.empty(int(np.prod(N)), dtype=torch.complex128, device=dev)
+        s = torch.cuda.current_stream(dev)
+        for _ in range(W):
+            plan.trafo_device(xd, fhd, P.COMPUTE_F, f=out_f, fixed_nodes=fixed)
+            plan.adj_device(xd, fd, f_hat=out_fh, fixed_nodes=fixed)
+        barrier()
+        evs = []
+        stage_b = [[], []]
+        for _ in range(K):
+            flush.fill_(1.0)  # L2 flush between timed steps (not timed)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            plan.trafo_device(xd, fhd, P.COMPUTE_F, f=out_f, fixed_nodes=fixed)
+            plan.adj_device(xd, fd, f_hat=out_fh, fixed_nodes=fixed)
+            b.record(s)
+            evs.append((a, b))
+            plan.synchronize()
+            stage_b[0].append(plan.stage_ms(False)[P.TIMER_MATRIX_B])
+            stage_b[1].append(plan.stage_ms(True)[P.TIMER_MATRIX_B])
+        barrier()
+        ms = [a.elapsed_time(b) for a, b in evs]
+        return ms, stage_b, out_f, out_fh
+
+    # --- FP32-mixed, device resident (headline value) ---------------------
+    p32 = P.Plan(N, n, m=m, precision="fp32")
+    sampler = ClockSampler()
+    sampler.start()
+    ms, stage_b, f32_out, fh32_out = device_steps(p32, args.steps, args.warmup)
+    clocks = sampler.stop()
+    step_ms = sum(ms) / len(ms)
+    t_max = torch.tensor([sum(ms)], device=dev)
+    if dist is not None:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+    value = world * M * args.steps / (t_max.item() * 1e-3) / 1e6
+
+    # amortised: nodes declared fixed (binning reused)
+    p32f = P.Plan(N, n, m=m, precision="fp32")
+    ms_fixed, _, _, _ = device_steps(p32f, max(3, args.steps // 2), 2, fixed=True)
+    p32f.close()
+
+    # --- dominant kernel roofline: interpolation B (trafo MATRIX_B) --------
+    b_ms = statistics.mean(stage_b[0])
+    bt_ms = statistics.mean(stage_b[1])
+    kern_ms, kname = (b_ms, "interp") if b_ms >= bt_ms else (bt_ms, "spread")
+    alg_bytes = M * (24 + 16) + int(np.prod(n)) * 8  # x (f64 x3) + f (c128) + grid (c64)
+    alg_flops = M * (2 * m + 1) ** 3 * 5
+    hbm, peak_kind = peaks()
+    achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
+    fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12
+    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": None, "kernel": f"k_{kname}_tile<float,13>", "kernel_ms": kern_ms,
+            "peak_source": peak_kind,
+            "alg_bytes_per_launch": alg_bytes, "alg_flops_per_launch": alg_flops,
+            "fp32_fma_tflops": alg_flops / (kern_ms * 1e-3) / 1e12,
+            "fp32_fma_frac_of_nominal": alg_flops / (kern_ms * 1e-3) / 1e12 / fp32_nominal,
+            "stage_ms": {"B": b_ms, "BT": bt_ms}}
+    traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic_file):
+        try:
+            with open(traffic_file) as fh_:
+                roof["traffic"] = json.load(fh_).get(roof["kernel"])
+        except Exception:
+            pass
+
+    # --- accuracy: FP32-mixed vs FP64 NDFT on 4096 nodes; adj vs FP64 path --
+    sub = 4096
+    pd = P.Plan(N, n, m=m, precision="fp64")
+    fd_direct, _, _ = pd.trafo_device(xd[:sub].contiguous(), fhd, P.COMPUTE_F | P.COMPUTE_DIRECT)
+    torch.cuda.synchronize()
+    err_trafo = (torch.linalg.vector_norm(f32_out[:sub] - fd_direct) / torch.linalg.vector_norm(fd_direct)).item()
+
+    # --- FP64 plain path -----------------------------------------------------
+    k64 = max(1, min(3, args.steps))
+    ms64, _, f64_out, fh64_out = device_steps(pd, k64, 1)
+    err_adj = (torch.linalg.vector_norm(fh32_out - fh64_out) / torch.linalg.vector_norm(fh64_out)).item()
+    err_trafo_64 = (torch.linalg.vector_norm(f64_out[:sub] - fd_direct) / torch.linalg.vector_norm(fd_direct)).item()
+    value64 = M / (statistics.mean(ms64) * 1e-3) / 1e6
+    pd.close()
+
+    # --- e2e through the C ABI on page-locked host arrays -------------------
+    L = P.load()
+    Nc = (ctypes.c_ssize_t * 3)(*N)
+    nc = (ctypes.c_ssize_t * 3)(*n)
+    xm = (ctypes.c_double * 3)(0.5, 0.5, 0.5)
+    plan = L.pnfft_init_guru(3, Nc, nc, xm, m, ctypes.c_uint(P.MALLOC_F_HAT | P.GB300_FP32), P.PFFT_ESTIMATE,
+                             P.MPI_COMM_WORLD)
+    nodes = L.pnfft_init_nodes(M, P.MALLOC_X | P.MALLOC_F)
+    hx = np.ctypeslib.as_array(ctypes.cast(L.pnfft_get_x(nodes), ctypes.POINTER(ctypes.c_double)), (M * 3,))
+    hf = np.ctypeslib.as_array(ctypes.cast(L.pnfft_get_f(nodes), ctypes.POINTER(ctypes.c_double)), (2 * M,))
+    hfh = np.ctypeslib.as_array(ctypes.cast(L.pnfft_get_f_hat(plan), ctypes.POINTER(ctypes.c_double)),
+                                (2 * fh.size,))
+    hx[:] = x.ravel()
+    fh_in = fh.view(np.float64)
+    f_in = f.view(np.float64)
+    for _ in range(args.warmup):
+        hfh[:] = fh_in
+        L.pnfft_trafo(plan, nodes, P.COMPUTE_F)
+        hf[:] = f_in
+        L.pnfft_adj(plan, nodes, P.COMPUTE_F)
+    barrier()
+    e2e_s = []
+    for _ in range(args.steps):
+        hfh[:] = fh_in  # (re)fill inputs outside the timed region
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        L.pnfft_trafo(plan, nodes, P.COMPUTE_F)
+        t1 = time.perf_counter()
+        hf[:] = f_in
+        t2 = time.perf_counter()
+        L.pnfft_adj(plan, nodes, P.COMPUTE_F)
+        t3 = time.perf_counter()
+        e2e_s.append((t1 - t0) + (t3 - t2))
+    barrier()
+    tsum = torch.tensor([sum(e2e_s)], device=dev)
+    if dist is not None:
+        dist.all_reduce(tsum, op=dist.ReduceOp.MAX)
+    e2e_value = world * M * args.steps / tsum.item() / 1e6
+    nfh = int(np.prod(N))
+    h2d = 2 * M * 24 + nfh * 16 + M * 16
+    d2h = M * 16 + nfh * 16
+    L.pnfft_free_nodes(nodes, P.FREE_X | P.FREE_F)
+    L.pnfft_finalize(plan, P.FREE_F_HAT)
+
+    launches_per_step = 12  # bin(4)+D+B  and  bin(4)+B^T+D^T  (cuFFT kernels not counted)
+    line = {"metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "N": list(N), "n": list(n), "M": M, "m": m,
+                       "window": "kaiser_bessel", "precision": "fp32-mixed (f64 index math and deconvolution)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "l2": "flushed between timed steps (258 MB write); inputs > L2"},
+            "e2e": {"value": e2e_value, "unit": "Mpts/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clocks, "roofline": roof,
+            "fp64": {"value": value64, "unit": "Mpts/s", "ms_per_step": statistics.mean(ms64),
+                     "err_trafo_vs_ndft": err_trafo_64},
+            "accuracy": {"fp32_trafo_rel_l2_vs_fp64_ndft_4096": err_trafo, "fp32_adj_rel_l2_vs_fp64_path": err_adj},
+            "amortised_fixed_nodes": {"value": M / (statistics.mean(ms_fixed) * 1e-3) / 1e6,
+                                      "ms_per_step": statistics.mean(ms_fixed)}}
+    if rank == 0 and world == 1 and not args.no_cpu:
+        line["cpu_baseline"] = {k: v for k, v in cpu_sample().items() if k != "seconds_per_step_extrapolated"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

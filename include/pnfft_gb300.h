@@ -1,0 +1,85 @@
+/*
+ * pnfft_gb300.h -- extensions of libpnfft_gb300 beyond the reference interface.
+ *
+ * These entry points have no counterpart in the reference (mpip/pnfft); they
+ * expose what a GPU implementation adds: error reporting, the arithmetic
+ * precision of the device path, device-resident (zero-copy) arrays and
+ * streams, and the bit-exact node sort for verification.
+ * Included by pnfft.h; may also be included alone.
+ */
+#ifndef PNFFT_GB300_H
+#define PNFFT_GB300_H 1
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#ifndef PNFFT_H
+typedef struct pnfft_plan_s *pnfft_plan;
+typedef struct pnfft_nodes_s *pnfft_nodes;
+#endif
+
+/* Precision of the device path of a plan.
+ *  PNFFT_GB300_FP64        all of D, F and B in FP64 (default).
+ *  PNFFT_GB300_FP32_MIXED  window values, spreading, interpolation and the FFT
+ *                          in FP32 with FP32 accumulation; node-to-grid index
+ *                          computation, the window Fourier coefficients of D
+ *                          and the host-facing arrays stay FP64.
+ * PNFFT_GB300_FP32 is a plan flag (a bit unused by the reference's flags)
+ * selecting the mixed form at pnfft_init_*. */
+#define PNFFT_GB300_FP64 0
+#define PNFFT_GB300_FP32_MIXED 1
+#define PNFFT_GB300_FP32 (1U << 30)
+
+/* Message of the last error recorded by any call (thread-local), or "" if none;
+ * pnfft_gb300_clear_error() resets it.  Errors never fall back to the CPU. */
+const char *pnfft_gb300_last_error(void);
+void pnfft_gb300_clear_error(void);
+
+/* Number of CUDA devices visible (0 when the driver has none). */
+int pnfft_gb300_device_count(void);
+
+/* Select / query the precision of a plan (returns 0 on success). */
+int pnfft_gb300_set_precision(pnfft_plan ths, int precision);
+int pnfft_gb300_get_precision(const pnfft_plan ths);
+
+/* Run the plan's work on a caller-owned cudaStream_t (NULL = the plan's own
+ * stream).  Returns 0 on success. */
+int pnfft_gb300_set_stream(pnfft_plan ths, void *cuda_stream);
+
+/* Zero-copy mode.  When device arrays are attached, pnfft_trafo/pnfft_adj read
+ * and write them directly and return without synchronizing the stream; the
+ * host pointers of the plan/nodes are not touched.  Layouts are those of the
+ * host arrays.  Pass NULL to detach (back to host arrays). */
+int pnfft_gb300_set_device_f_hat(pnfft_plan ths, void *d_f_hat);
+int pnfft_gb300_set_device_arrays(pnfft_nodes nodes, double *d_x, void *d_f, void *d_grad_f, void *d_hessian_f);
+
+/* Promise that the node coordinates do not change until the next call with
+ * fixed=0 (or until pnfft_set_x / pnfft_gb300_set_device_arrays): the binning
+ * of the nodes onto grid tiles is then computed once and reused.
+ * pnfft_precompute_psi implies the same promise, as in the reference. */
+int pnfft_gb300_nodes_set_fixed(pnfft_nodes nodes, int fixed);
+
+/* Wait for all work of the plan's stream (returns 0 on success). */
+int pnfft_gb300_synchronize(pnfft_plan ths);
+
+/* Verification entry points (host arrays in and out, run on the GPU):
+ *  - the sort of PNFFT_SORT_NODES: pairs[2p] = key of the p-th node in sorted
+ *    order, pairs[2p+1] = its original index (stable, bit-exact with the
+ *    reference's radix sort, kernel/ndft-parallel.c:2121-2159);
+ *  - the lowest grid index floor(n_t x_t) - m of every node (with the
+ *    interlacing shift when interlaced != 0), kernel/ndft-parallel.c:2165-2174. */
+int pnfft_gb300_sort_nodes(pnfft_plan ths, ptrdiff_t M, const double *x, long long *pairs);
+int pnfft_gb300_node_index(pnfft_plan ths, ptrdiff_t M, const double *x, int interlaced, long long *u);
+
+/* Milliseconds of the stages of the last pnfft_trafo / pnfft_adj of the plan,
+ * indexed like the PNFFT_TIMER_* constants. */
+int pnfft_gb300_last_stage_ms(const pnfft_plan ths, int adjoint, double *ms10);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* PNFFT_GB300_H */

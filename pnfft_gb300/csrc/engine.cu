@@ -1,0 +1,805 @@
+// engine.cu -- device side of pnfft_trafo / pnfft_adj: buffers, cuFFT plans,
+// stage timing, and the orchestration of api/api-basic.c:100-378 on one GPU.
+//
+//   trafo: [bin nodes] -> D (+pad) -> FFT -> B          (api-basic.c:170-196)
+//          DIFF_IK: one D/FFT/B pass per output component (100-167)
+//          INTERLACED: a second, shifted pass, each scaled by 1/2 (233-240)
+//   adj:   [bin nodes] -> B^T -> FFT^H -> D^T (+crop)   (307-333)
+//          DIFF_IK: one B^T/FFT^H/D^T pass per input component (249-305)
+// The PFFT transposes and ghost-cell exchanges of the reference have no
+// counterpart: the grid is one n0 x n1 x n2 array in HBM.
+#include <cuda_runtime.h>
+#include <cufft.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <unordered_set>
+
+#include "pg_internal.h"
+#include "pg_kernels.h"
+
+namespace pg {
+
+#define PG_CUDA(call)                                                                             \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) {                                                                      \
+      set_error("CUDA error %s at %s:%d: %s", cudaGetErrorName(e_), __FILE__, __LINE__,           \
+                cudaGetErrorString(e_));                                                          \
+      return -1;                                                                                  \
+    }                                                                                             \
+  } while (0)
+
+#define PG_FFT(call)                                                                              \
+  do {                                                                                            \
+    cufftResult r_ = (call);                                                                      \
+    if (r_ != CUFFT_SUCCESS) {                                                                    \
+      set_error("cuFFT error %d at %s:%d", (int)r_, __FILE__, __LINE__);                         \
+      return -1;                                                                                  \
+    }                                                                                             \
+  } while (0)
+
+static const unsigned C_F = PNFFT_COMPUTE_F, C_GRAD = PNFFT_COMPUTE_GRAD_F, C_HESS = PNFFT_COMPUTE_HESSIAN_F;
+
+struct Stage {
+  int idx;  // PNFFT_TIMER_*
+  int adj;
+  cudaEvent_t a, b;
+};
+
+struct DevState {
+  int device = -1;
+  cudaStream_t own = nullptr, stream = nullptr;
+  void *grid = nullptr;
+  size_t grid_bytes = 0;
+  cufftHandle fft = 0;
+  int fft_prec = -1;
+  double *inv[3] = {nullptr, nullptr, nullptr};
+  void *tab[3][3] = {{nullptr}};
+  uint64_t tables_for = ~0ull;
+  double *fhat = nullptr;
+  size_t fhat_cap = 0;
+  // binning scratch for the plain and the interlaced pass
+  Binning bin[2] = {};
+  int64_t bin_cap_M = 0;
+  int bin_T[3] = {0, 0, 0};
+  int bin_prec = -1;
+  uint64_t bin_uid[2] = {0, 0}, bin_ver[2] = {0, 0};
+  bool bin_valid[2] = {false, false};
+  std::vector<Stage> pending;
+  std::vector<cudaEvent_t> free_ev;
+};
+
+struct NodeDev {
+  double *x = nullptr, *f = nullptr, *grad = nullptr, *hess = nullptr;
+  int64_t cap = 0;
+};
+
+// ---------------------------------------------------------------------------
+// host memory of pnfft_malloc: page-locked when a device is present
+// ---------------------------------------------------------------------------
+static std::mutex g_pin_mu;
+static std::unordered_set<void *> g_pinned;
+
+int engine_device_count() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+void *engine_host_alloc(size_t bytes) {
+  if (bytes == 0) return nullptr;
+  void *p = nullptr;
+  if (engine_device_count() > 0 && cudaMallocHost(&p, bytes) == cudaSuccess) {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    g_pinned.insert(p);
+    return p;
+  }
+  cudaGetLastError();
+  return nullptr;
+}
+
+bool engine_host_free(void *p) {
+  {
+    std::lock_guard<std::mutex> lk(g_pin_mu);
+    auto it = g_pinned.find(p);
+    if (it == g_pinned.end()) return false;
+    g_pinned.erase(it);
+  }
+  cudaFreeHost(p);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// device state
+// ---------------------------------------------------------------------------
+static int ensure_dev(pnfft_plan p) {
+  if (!p->dev) p->dev = new DevState();
+  DevState *d = p->dev;
+  if (d->device < 0) {
+    int n = engine_device_count();
+    if (n <= 0) {
+      set_error("libpnfft_gb300: no CUDA device is visible; this library has no CPU path");
+      return -1;
+    }
+    PG_CUDA(cudaGetDevice(&d->device));
+    PG_CUDA(cudaStreamCreateWithFlags(&d->own, cudaStreamNonBlocking));
+  }
+  d->stream = p->user_stream ? (cudaStream_t)p->user_stream : d->own;
+  return 0;
+}
+
+static bool fp32(pnfft_plan p) { return p->precision == PNFFT_GB300_FP32_MIXED; }
+static size_t celem(pnfft_plan p) { return fp32(p) ? 8 : 16; }
+
+static int ensure_grid_fft(pnfft_plan p) {
+  DevState *d = p->dev;
+  size_t bytes = (size_t)p->n[0] * p->n[1] * p->n[2] * celem(p);
+  if (d->grid_bytes < bytes) {
+    if (d->grid) cudaFree(d->grid);
+    d->grid = nullptr;
+    d->grid_bytes = 0;
+    PG_CUDA(cudaMalloc(&d->grid, bytes));
+    d->grid_bytes = bytes;
+  }
+  if (d->fft_prec != p->precision) {
+    if (d->fft_prec >= 0) cufftDestroy(d->fft);
+    d->fft_prec = -1;
+    PG_FFT(cufftPlan3d(&d->fft, (int)p->n[0], (int)p->n[1], (int)p->n[2], fp32(p) ? CUFFT_C2C : CUFFT_Z2Z));
+    d->fft_prec = p->precision;
+  }
+  PG_FFT(cufftSetStream(d->fft, d->stream));
+  return 0;
+}
+
+static int ensure_tables(pnfft_plan p) {
+  DevState *d = p->dev;
+  uint64_t want = (p->table_version << 1) | (uint64_t)(fp32(p) ? 1 : 0);
+  if (d->tables_for == want) return 0;
+  for (int t = 0; t < 3; t++) {
+    if (d->inv[t]) cudaFree(d->inv[t]);
+    d->inv[t] = nullptr;
+    size_t nb = sizeof(double) * p->inv[t].size();
+    PG_CUDA(cudaMalloc(&d->inv[t], nb > 0 ? nb : 8));
+    PG_CUDA(cudaMemcpy(d->inv[t], p->inv[t].data(), nb, cudaMemcpyHostToDevice));
+  }
+  for (int der = 0; der < 3; der++)
+    for (int t = 0; t < 3; t++) {
+      if (d->tab[der][t]) cudaFree(d->tab[der][t]);
+      d->tab[der][t] = nullptr;
+      const std::vector<double> &h = p->tab[der][t];
+      if (h.empty()) continue;
+      if (fp32(p)) {
+        std::vector<float> tmp(h.begin(), h.end());
+        PG_CUDA(cudaMalloc(&d->tab[der][t], sizeof(float) * tmp.size()));
+        PG_CUDA(cudaMemcpy(d->tab[der][t], tmp.data(), sizeof(float) * tmp.size(), cudaMemcpyHostToDevice));
+      } else {
+        PG_CUDA(cudaMalloc(&d->tab[der][t], sizeof(double) * h.size()));
+        PG_CUDA(cudaMemcpy(d->tab[der][t], h.data(), sizeof(double) * h.size(), cudaMemcpyHostToDevice));
+      }
+    }
+  d->tables_for = want;
+  return 0;
+}
+
+static void free_binning(Binning &b) {
+  int **arrs[] = {&b.key, &b.perm, &b.count, &b.start, &b.cursor, &b.nsub_tile, &b.sub_off, &b.sub_tile,
+                  &b.sub_first, &b.sub_cnt, &b.nsub};
+  for (int **a : arrs) {
+    if (*a) cudaFree(*a);
+    *a = nullptr;
+  }
+}
+
+static int ensure_binning(pnfft_plan p, int64_t M) {
+  DevState *d = p->dev;
+  int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
+  int T[3];
+  choose_tiles(p->cutoff, fp32(p), n, T);
+  bool same_tiles = T[0] == d->bin_T[0] && T[1] == d->bin_T[1] && T[2] == d->bin_T[2];
+  if (same_tiles && d->bin_cap_M >= M && d->bin[0].key) return 0;
+  int64_t cap = std::max<int64_t>(M, std::max<int64_t>(d->bin_cap_M, 1));
+  for (int ps = 0; ps < 2; ps++) {
+    Binning &b = d->bin[ps];
+    free_binning(b);
+    for (int t = 0; t < 3; t++) {
+      b.T[t] = T[t];
+      b.ntile[t] = (n[t] + T[t] - 1) / T[t];
+    }
+    b.ntiles = b.ntile[0] * b.ntile[1] * b.ntile[2];
+    b.sub_max = 1024;
+    b.max_subs = (int)(b.ntiles + cap / b.sub_max + 1);
+    PG_CUDA(cudaMalloc(&b.key, sizeof(int) * cap));
+    PG_CUDA(cudaMalloc(&b.perm, sizeof(int) * cap));
+    PG_CUDA(cudaMalloc(&b.count, sizeof(int) * b.ntiles));
+    PG_CUDA(cudaMalloc(&b.start, sizeof(int) * b.ntiles));
+    PG_CUDA(cudaMalloc(&b.cursor, sizeof(int) * b.ntiles));
+    PG_CUDA(cudaMalloc(&b.nsub_tile, sizeof(int) * b.ntiles));
+    PG_CUDA(cudaMalloc(&b.sub_off, sizeof(int) * b.ntiles));
+    PG_CUDA(cudaMalloc(&b.sub_tile, sizeof(int) * b.max_subs));
+    PG_CUDA(cudaMalloc(&b.sub_first, sizeof(int) * b.max_subs));
+    PG_CUDA(cudaMalloc(&b.sub_cnt, sizeof(int) * b.max_subs));
+    PG_CUDA(cudaMalloc(&b.nsub, sizeof(int)));
+    d->bin_valid[ps] = false;
+  }
+  d->bin_cap_M = cap;
+  for (int t = 0; t < 3; t++) d->bin_T[t] = T[t];
+  return 0;
+}
+
+static int ensure_node_buffers(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
+  if (!nd->dev) nd->dev = new NodeDev();
+  NodeDev *v = nd->dev;
+  int64_t M = nd->local_M;
+  if (v->cap < M) {
+    cudaFree(v->x);
+    cudaFree(v->f);
+    cudaFree(v->grad);
+    cudaFree(v->hess);
+    v->x = v->f = v->grad = v->hess = nullptr;
+    v->cap = 0;
+    size_t m = (size_t)std::max<int64_t>(M, 1);
+    PG_CUDA(cudaMalloc(&v->x, sizeof(double) * 3 * m));
+    PG_CUDA(cudaMalloc(&v->f, sizeof(double) * 2 * m));
+    v->cap = M;
+  }
+  size_t m = (size_t)std::max<int64_t>(v->cap, 1);
+  if ((cflags & C_GRAD) && !v->grad) PG_CUDA(cudaMalloc(&v->grad, sizeof(double) * 6 * m));
+  if ((cflags & C_HESS) && !v->hess) PG_CUDA(cudaMalloc(&v->hess, sizeof(double) * 12 * m));
+  (void)p;
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// stage timers (CUDA events on the plan's stream)
+// ---------------------------------------------------------------------------
+static cudaEvent_t get_event(DevState *d) {
+  if (!d->free_ev.empty()) {
+    cudaEvent_t e = d->free_ev.back();
+    d->free_ev.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+struct StageScope {
+  DevState *d;
+  Stage st;
+  StageScope(DevState *d_, int idx, int adj) : d(d_) {
+    st.idx = idx;
+    st.adj = adj;
+    st.a = get_event(d);
+    st.b = get_event(d);
+    cudaEventRecord(st.a, d->stream);
+  }
+  ~StageScope() {
+    cudaEventRecord(st.b, d->stream);
+    d->pending.push_back(st);
+  }
+};
+
+void engine_flush_timers(pnfft_plan p) {
+  DevState *d = p->dev;
+  if (!d || d->pending.empty()) return;
+  cudaStreamSynchronize(d->stream);
+  bool seen[2] = {false, false};
+  for (const Stage &s : d->pending) {
+    if (!seen[s.adj]) {
+      for (int i = 0; i < PNFFT_TIMER_LENGTH; i++) p->last_ms[s.adj][i] = 0;
+      seen[s.adj] = true;
+    }
+    float ms = 0;
+    if (cudaEventElapsedTime(&ms, s.a, s.b) == cudaSuccess) {
+      double *tm = s.adj ? p->timer_adj : p->timer_trafo;
+      tm[s.idx] += ms * 1e-3;
+      p->last_ms[s.adj][s.idx] += ms;
+    }
+    d->free_ev.push_back(s.a);
+    d->free_ev.push_back(s.b);
+  }
+  cudaGetLastError();
+  d->pending.clear();
+}
+
+// ---------------------------------------------------------------------------
+// building blocks
+// ---------------------------------------------------------------------------
+static WindowArgs window_args(pnfft_plan p) {
+  WindowArgs w;
+  w.kind = p->window;
+  w.m = p->m;
+  w.cut = p->cutoff;
+  for (int t = 0; t < 3; t++) {
+    w.n[t] = (int)p->n[t];
+    w.b[t] = p->b[t];
+  }
+  w.intpol_order = p->intpol_order;
+  w.intpol_K = (int)p->intpol_K;
+  for (int der = 0; der < 3; der++)
+    for (int t = 0; t < 3; t++) w.tab[der][t] = p->dev->tab[der][t];
+  return w;
+}
+
+static DeconvArgs deconv_args(pnfft_plan p) {
+  DeconvArgs a;
+  memset(&a, 0, sizeof(a));
+  for (int t = 0; t < 3; t++) {
+    a.N[t] = (int)p->N[t];
+    a.n[t] = (int)p->n[t];
+    a.Nl[t] = p->local_N[t];
+    a.ks[t] = p->local_N_start[t];
+    a.inv[t] = p->dev->inv[t];
+  }
+  a.transposed = (p->pnfft_flags & PNFFT_TRANSPOSED_F_HAT) ? 1 : 0;
+  a.c2r = p->c2r;
+  a.grid = p->dev->grid;
+  return a;
+}
+
+static int fft_exec(pnfft_plan p, int direction) {
+  DevState *d = p->dev;
+  if (fp32(p)) PG_FFT(cufftExecC2C(d->fft, (cufftComplex *)d->grid, (cufftComplex *)d->grid, direction));
+  else PG_FFT(cufftExecZ2Z(d->fft, (cufftDoubleComplex *)d->grid, (cufftDoubleComplex *)d->grid, direction));
+  return 0;
+}
+
+// bins the nodes for pass `il` unless a valid binning of the same fixed nodes exists
+static int do_binning(pnfft_plan p, pnfft_nodes nd, ConvArgs &a, int il, int adj) {
+  DevState *d = p->dev;
+  a.bin = d->bin[il];
+  bool reuse = nd->fixed && d->bin_valid[il] && d->bin_uid[il] == nd->uid && d->bin_ver[il] == nd->version;
+  if (!reuse) {
+    StageScope sc(d, PNFFT_TIMER_SORT_NODES, adj);
+    bin_nodes(a, d->stream);
+    d->bin_valid[il] = true;
+    d->bin_uid[il] = nd->uid;
+    d->bin_ver[il] = nd->version;
+  }
+  return 0;
+}
+
+struct Arrays {
+  const double *x;
+  double *f, *grad, *hess;  // node arrays on the device
+  double *fhat;             // f_hat on the device
+};
+
+static int resolve_arrays(pnfft_plan p, pnfft_nodes nd, unsigned cflags, bool adjoint, Arrays &A, bool &zero_copy) {
+  DevState *d = p->dev;
+  int64_t M = nd ? nd->local_M : 0;
+  const int tuple = p->c2r ? 1 : 2;
+  zero_copy = nd && nd->u_x;
+  if (nd) {
+    if (zero_copy) {
+      A.x = nd->u_x;
+      A.f = (double *)nd->u_f;
+      A.grad = (double *)nd->u_grad;
+      A.hess = (double *)nd->u_hess;
+    } else {
+      if (ensure_node_buffers(p, nd, cflags)) return -1;
+      NodeDev *v = nd->dev;
+      A.x = v->x;
+      A.f = v->f;
+      A.grad = v->grad;
+      A.hess = v->hess;
+      if (M > 0) {
+        if (!nd->x) {
+          set_error("pnfft: nodes->x is not allocated");
+          return -1;
+        }
+        if (!adjoint) {
+          if ((cflags & C_F) && !nd->f) return set_error("pnfft_trafo: missing memory allocation of nodes->f"), -1;
+          if ((cflags & C_GRAD) && !nd->grad_f)
+            return set_error("pnfft_trafo: missing memory allocation of nodes->grad_f"), -1;
+          if ((cflags & C_HESS) && !nd->hessian_f)
+            return set_error("pnfft_trafo: missing memory allocation of nodes->hessian_f"), -1;
+        }
+        PG_CUDA(cudaMemcpyAsync(v->x, nd->x, sizeof(double) * 3 * M, cudaMemcpyHostToDevice, d->stream));
+        bool upload_out = !adjoint && (cflags & PNFFT_COMPUTE_ACCUMULATED);
+        if ((cflags & C_F) && (adjoint || upload_out)) {
+          if (!nd->f) {
+            set_error("pnfft: missing memory allocation of nodes->f");
+            return -1;
+          }
+          PG_CUDA(cudaMemcpyAsync(v->f, nd->f, sizeof(double) * tuple * M, cudaMemcpyHostToDevice, d->stream));
+        }
+        if ((cflags & C_GRAD) && (adjoint || upload_out)) {
+          if (!nd->grad_f) {
+            set_error("pnfft: missing memory allocation of nodes->grad_f");
+            return -1;
+          }
+          PG_CUDA(cudaMemcpyAsync(v->grad, nd->grad_f, sizeof(double) * 3 * tuple * M, cudaMemcpyHostToDevice,
+                                  d->stream));
+        }
+        if (!adjoint && (cflags & C_HESS) && upload_out) {
+          if (!nd->hessian_f) {
+            set_error("pnfft: missing memory allocation of nodes->hessian_f");
+            return -1;
+          }
+          PG_CUDA(cudaMemcpyAsync(v->hess, nd->hessian_f, sizeof(double) * 6 * tuple * M, cudaMemcpyHostToDevice,
+                                  d->stream));
+        }
+      }
+    }
+  } else {
+    A.x = nullptr;
+    A.f = A.grad = A.hess = nullptr;
+  }
+  // f_hat
+  size_t fb = sizeof(double) * 2 * (size_t)p->local_N_total;
+  if (p->d_f_hat_user) {
+    A.fhat = (double *)p->d_f_hat_user;
+  } else {
+    if (d->fhat_cap < fb) {
+      if (d->fhat) cudaFree(d->fhat);
+      d->fhat = nullptr;
+      d->fhat_cap = 0;
+      PG_CUDA(cudaMalloc(&d->fhat, fb > 0 ? fb : 16));
+      d->fhat_cap = fb;
+    }
+    A.fhat = d->fhat;
+    bool need_in = !adjoint || (cflags & PNFFT_COMPUTE_ACCUMULATED);
+    if (need_in && fb > 0) {
+      if (!p->f_hat) {
+        set_error("pnfft: f_hat is not allocated");
+        return -1;
+      }
+      PG_CUDA(cudaMemcpyAsync(d->fhat, p->f_hat, fb, cudaMemcpyHostToDevice, d->stream));
+    }
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// pnfft_trafo
+// ---------------------------------------------------------------------------
+int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
+  if (ensure_dev(p)) return -1;
+  DevState *d = p->dev;
+  cudaStream_t s = d->stream;
+  if (ensure_grid_fft(p) || ensure_tables(p)) return -1;
+  int64_t M = nd ? nd->local_M : 0;
+  if (ensure_binning(p, M)) return -1;
+  const int tuple = p->c2r ? 1 : 2;
+  Arrays A;
+  bool zc = false;
+  {
+    StageScope whole(d, PNFFT_TIMER_WHOLE, 0);
+    if (resolve_arrays(p, nd, cflags, false, A, zc)) return -1;
+    // zero the outputs (api-basic.c:210-222; trafo_A always overwrites, 400-414)
+    bool zero = (!(cflags & PNFFT_COMPUTE_ACCUMULATED) && !(cflags & PNFFT_OMIT_CONV)) ||
+                (cflags & PNFFT_COMPUTE_DIRECT);
+    if (zero && M > 0) {
+      if ((cflags & C_F) && A.f) PG_CUDA(cudaMemsetAsync(A.f, 0, sizeof(double) * tuple * M, s));
+      if ((cflags & C_GRAD) && A.grad) PG_CUDA(cudaMemsetAsync(A.grad, 0, sizeof(double) * 3 * tuple * M, s));
+      if ((cflags & C_HESS) && A.hess) PG_CUDA(cudaMemsetAsync(A.hess, 0, sizeof(double) * 6 * tuple * M, s));
+    }
+    if ((cflags & C_F) && M > 0 && !A.f) return set_error("pnfft_trafo: missing memory allocation of nodes->f"), -1;
+    if ((cflags & C_GRAD) && M > 0 && !A.grad)
+      return set_error("pnfft_trafo: missing memory allocation of nodes->grad_f"), -1;
+    if ((cflags & C_HESS) && M > 0 && !A.hess)
+      return set_error("pnfft_trafo: missing memory allocation of nodes->hessian_f"), -1;
+
+    if (cflags & PNFFT_COMPUTE_DIRECT) {
+      NdftArgs na;
+      memset(&na, 0, sizeof(na));
+      for (int t = 0; t < 3; t++) {
+        na.N[t] = (int)p->N[t];
+        na.Nl[t] = p->local_N[t];
+        na.ks[t] = p->local_N_start[t];
+      }
+      na.transposed = (p->pnfft_flags & PNFFT_TRANSPOSED_F_HAT) ? 1 : 0;
+      na.c2r = p->c2r;
+      na.M = M;
+      na.x = A.x;
+      na.fhat = A.fhat;
+      na.f = A.f;
+      na.grad = A.grad;
+      na.hess = A.hess;
+      na.cflags = cflags;
+      launch_ndft_trafo(na, s);
+    } else {
+      const bool il_plan = (p->pnfft_flags & PNFFT_INTERLACED) != 0;
+      const bool ik = (p->pnfft_flags & PNFFT_DIFF_IK) != 0;
+      const bool f32 = fp32(p);
+      ConvArgs ca;
+      memset(&ca, 0, sizeof(ca));
+      ca.w = window_args(p);
+      ca.real_only = p->c2r || (p->pnfft_flags & PNFFT_PRE_QUAD_PSI) ? 1 : 0;
+      ca.real_io = p->c2r;
+      ca.M = M;
+      ca.x = A.x;
+      ca.grid = d->grid;
+      DeconvArgs da = deconv_args(p);
+      da.fhat_in = A.fhat;
+      for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
+        const int il = il_plan ? pass : 0;
+        ca.use_il = il_plan ? 1 : 0;
+        ca.il = il;
+        da.interlaced = il;
+        if (nd && !(cflags & PNFFT_OMIT_CONV)) do_binning(p, nd, ca, il, 0);
+        auto one = [&](int ikmode, int ikdim, double *out, int64_t off, int64_t stride, int mode) -> int {
+          {
+            StageScope sc(d, PNFFT_TIMER_MATRIX_D, 0);
+            da.ik = ikmode;
+            da.ik_dim = ikdim;
+            if (!(cflags & PNFFT_OMIT_DECONV)) launch_deconv_pad(da, f32, s);
+          }
+          {
+            StageScope sc(d, PNFFT_TIMER_MATRIX_F, 0);
+            if (!(cflags & PNFFT_OMIT_FFT) && fft_exec(p, CUFFT_FORWARD)) return -1;
+          }
+          if (!(cflags & PNFFT_OMIT_CONV) && nd) {
+            StageScope sc(d, PNFFT_TIMER_MATRIX_B, 0);
+            ConvArgs c = ca;
+            c.offset = off;
+            c.stride = stride;
+            if (mode & 4) {
+              c.hess_out = out;
+              launch_interp(c, 4, f32, s);
+            } else if (mode == 1) {
+              c.f_out = out;
+              launch_interp(c, 1, f32, s);
+            }
+          }
+          return 0;
+        };
+        if (ik) {
+          if ((cflags & C_F) && one(0, 0, A.f, 0, 1, 1)) return -1;
+          if (cflags & C_GRAD)
+            for (int dim = 0; dim < 3; dim++)
+              if (one(1, dim, A.grad, dim, 3, 1)) return -1;
+          if (cflags & C_HESS)
+            for (int dim = 0; dim < 6; dim++)
+              if (one(2, dim, A.hess, dim, 6, 1)) return -1;
+        } else {
+          {
+            StageScope sc(d, PNFFT_TIMER_MATRIX_D, 0);
+            da.ik = 0;
+            if (!(cflags & PNFFT_OMIT_DECONV)) launch_deconv_pad(da, f32, s);
+          }
+          {
+            StageScope sc(d, PNFFT_TIMER_MATRIX_F, 0);
+            if (!(cflags & PNFFT_OMIT_FFT) && fft_exec(p, CUFFT_FORWARD)) return -1;
+          }
+          if (!(cflags & PNFFT_OMIT_CONV) && nd) {
+            StageScope sc(d, PNFFT_TIMER_MATRIX_B, 0);
+            ConvArgs c = ca;
+            c.offset = 0;
+            c.stride = 1;
+            c.f_out = A.f;
+            c.grad_out = A.grad;
+            c.hess_out = A.hess;
+            int mode = ((cflags & C_F) ? 1 : 0) | ((cflags & C_GRAD) ? 2 : 0);
+            if (mode) launch_interp(c, mode, f32, s);
+            if (cflags & C_HESS) launch_interp(c, 4, f32, s);
+          }
+        }
+      }
+    }
+    if (!zc && M > 0) {
+      if (cflags & C_F) PG_CUDA(cudaMemcpyAsync(nd->f, A.f, sizeof(double) * tuple * M, cudaMemcpyDeviceToHost, s));
+      if (cflags & C_GRAD)
+        PG_CUDA(cudaMemcpyAsync(nd->grad_f, A.grad, sizeof(double) * 3 * tuple * M, cudaMemcpyDeviceToHost, s));
+      if (cflags & C_HESS)
+        PG_CUDA(cudaMemcpyAsync(nd->hessian_f, A.hess, sizeof(double) * 6 * tuple * M, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  p->timer_trafo[PNFFT_TIMER_ITER] += 1;
+  PG_CUDA(cudaGetLastError());
+  if (!(zc || !nd) || !p->d_f_hat_user) {
+    PG_CUDA(cudaStreamSynchronize(s));
+    engine_flush_timers(p);
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// pnfft_adj
+// ---------------------------------------------------------------------------
+int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
+  if (ensure_dev(p)) return -1;
+  DevState *d = p->dev;
+  cudaStream_t s = d->stream;
+  if (ensure_grid_fft(p) || ensure_tables(p)) return -1;
+  int64_t M = nd ? nd->local_M : 0;
+  if (ensure_binning(p, M)) return -1;
+  Arrays A;
+  bool zc = false;
+  size_t fb = sizeof(double) * 2 * (size_t)p->local_N_total;
+  {
+    StageScope whole(d, PNFFT_TIMER_WHOLE, 1);
+    if (resolve_arrays(p, nd, cflags, true, A, zc)) return -1;
+    if (!(cflags & PNFFT_COMPUTE_ACCUMULATED) && fb > 0) PG_CUDA(cudaMemsetAsync(A.fhat, 0, fb, s));
+    if ((cflags & C_F) && M > 0 && !A.f) return set_error("pnfft_adj: missing memory allocation of nodes->f"), -1;
+    if ((cflags & C_GRAD) && M > 0 && !A.grad)
+      return set_error("pnfft_adj: missing memory allocation of nodes->grad_f"), -1;
+
+    if (cflags & PNFFT_COMPUTE_DIRECT) {
+      NdftArgs na;
+      memset(&na, 0, sizeof(na));
+      for (int t = 0; t < 3; t++) {
+        na.N[t] = (int)p->N[t];
+        na.Nl[t] = p->local_N[t];
+        na.ks[t] = p->local_N_start[t];
+      }
+      na.transposed = (p->pnfft_flags & PNFFT_TRANSPOSED_F_HAT) ? 1 : 0;
+      na.c2r = p->c2r;
+      na.M = M;
+      na.x = A.x;
+      na.f_in = A.f;
+      na.grad_in = A.grad;
+      na.fhat_out = A.fhat;
+      na.cflags = cflags;
+      launch_ndft_adj(na, s);
+    } else {
+      const bool il_plan = (p->pnfft_flags & PNFFT_INTERLACED) != 0;
+      const bool ik = (p->pnfft_flags & PNFFT_DIFF_IK) != 0;
+      const bool f32 = fp32(p);
+      const size_t gbytes = (size_t)p->n[0] * p->n[1] * p->n[2] * celem(p);
+      ConvArgs ca;
+      memset(&ca, 0, sizeof(ca));
+      ca.w = window_args(p);
+      ca.real_only = 0;
+      ca.real_io = p->c2r;
+      ca.M = M;
+      ca.x = A.x;
+      ca.grid = d->grid;
+      DeconvArgs da = deconv_args(p);
+      da.fhat_out = A.fhat;
+      for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
+        const int il = il_plan ? pass : 0;
+        ca.use_il = il_plan ? 1 : 0;
+        ca.il = il;
+        da.interlaced = il;
+        if (nd && !(cflags & PNFFT_OMIT_CONV)) do_binning(p, nd, ca, il, 1);
+        auto one = [&](int ikmode, int ikdim, const double *fin, const double *gin, int64_t off, int64_t stride,
+                       int mode) -> int {
+          {
+            StageScope sc(d, PNFFT_TIMER_MATRIX_B, 1);
+            PG_CUDA(cudaMemsetAsync(d->grid, 0, gbytes, s));
+            if (!(cflags & PNFFT_OMIT_CONV) && nd) {
+              ConvArgs c = ca;
+              c.offset = off;
+              c.stride = stride;
+              c.f_in = fin;
+              c.grad_in = gin;
+              launch_spread(c, mode, f32, s);
+            }
+          }
+          {
+            StageScope sc(d, PNFFT_TIMER_MATRIX_F, 1);
+            if (!(cflags & PNFFT_OMIT_FFT) && fft_exec(p, CUFFT_INVERSE)) return -1;
+          }
+          {
+            StageScope sc(d, PNFFT_TIMER_MATRIX_D, 1);
+            da.ik = ikmode;
+            da.ik_dim = ikdim;
+            if (!(cflags & PNFFT_OMIT_DECONV)) launch_deconv_crop_acc(da, f32, s);
+          }
+          return 0;
+        };
+        if (ik) {
+          if ((cflags & C_F) && one(0, 0, A.f, nullptr, 0, 1, 1)) return -1;
+          if (cflags & C_GRAD)
+            for (int dim = 0; dim < 3; dim++)
+              if (one(1, dim, A.grad, nullptr, dim, 3, 1)) return -1;
+        } else {
+          int mode = ((cflags & C_F) ? 1 : 0) | ((cflags & C_GRAD) ? 2 : 0);
+          if (mode && one(0, 0, A.f, A.grad, 0, 1, mode)) return -1;
+        }
+      }
+    }
+    if (!p->d_f_hat_user && fb > 0) {
+      if (!p->f_hat) return set_error("pnfft_adj: f_hat is not allocated"), -1;
+      PG_CUDA(cudaMemcpyAsync(p->f_hat, A.fhat, fb, cudaMemcpyDeviceToHost, s));
+    }
+  }
+  p->timer_adj[PNFFT_TIMER_ITER] += 1;
+  PG_CUDA(cudaGetLastError());
+  if (!(zc || !nd) || !p->d_f_hat_user) {
+    PG_CUDA(cudaStreamSynchronize(s));
+    engine_flush_timers(p);
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// misc
+// ---------------------------------------------------------------------------
+int engine_set_stream(pnfft_plan p, void *stream) {
+  p->user_stream = stream;
+  if (p->dev && p->dev->device >= 0) {
+    p->dev->stream = stream ? (cudaStream_t)stream : p->dev->own;
+    if (p->dev->fft_prec >= 0) PG_FFT(cufftSetStream(p->dev->fft, p->dev->stream));
+  }
+  return 0;
+}
+
+int engine_sync(pnfft_plan p) {
+  if (!p->dev || p->dev->device < 0) return 0;
+  PG_CUDA(cudaStreamSynchronize(p->dev->stream));
+  engine_flush_timers(p);
+  return 0;
+}
+
+void engine_release_plan(pnfft_plan p) {
+  DevState *d = p->dev;
+  if (!d) return;
+  if (d->device >= 0) {
+    cudaStreamSynchronize(d->stream);
+    d->pending.clear();
+    if (d->grid) cudaFree(d->grid);
+    if (d->fft_prec >= 0) cufftDestroy(d->fft);
+    for (int t = 0; t < 3; t++)
+      if (d->inv[t]) cudaFree(d->inv[t]);
+    for (int a = 0; a < 3; a++)
+      for (int t = 0; t < 3; t++)
+        if (d->tab[a][t]) cudaFree(d->tab[a][t]);
+    if (d->fhat) cudaFree(d->fhat);
+    for (int ps = 0; ps < 2; ps++) free_binning(d->bin[ps]);
+    for (cudaEvent_t e : d->free_ev) cudaEventDestroy(e);
+    if (d->own) cudaStreamDestroy(d->own);
+    cudaGetLastError();
+  }
+  delete d;
+  p->dev = nullptr;
+}
+
+void engine_release_nodes(pnfft_nodes nd) {
+  NodeDev *v = nd->dev;
+  if (!v) return;
+  cudaFree(v->x);
+  cudaFree(v->f);
+  cudaFree(v->grad);
+  cudaFree(v->hess);
+  cudaGetLastError();
+  delete v;
+  nd->dev = nullptr;
+}
+
+int engine_sort_nodes(pnfft_plan p, int64_t M, const double *x, long long *pairs) {
+  if (ensure_dev(p)) return -1;
+  cudaStream_t s = p->dev->stream;
+  if (M <= 0) return 0;
+  double *dx = nullptr;
+  long long *dp = nullptr;
+  PG_CUDA(cudaMallocAsync(&dx, sizeof(double) * 3 * M, s));
+  PG_CUDA(cudaMallocAsync(&dp, sizeof(long long) * 2 * M, s));
+  PG_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * 3 * M, cudaMemcpyHostToDevice, s));
+  int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
+  int rc = radix_sort_nodes(dx, M, n, p->m, dp, s);
+  if (rc == 0) PG_CUDA(cudaMemcpyAsync(pairs, dp, sizeof(long long) * 2 * M, cudaMemcpyDeviceToHost, s));
+  cudaFreeAsync(dx, s);
+  cudaFreeAsync(dp, s);
+  PG_CUDA(cudaStreamSynchronize(s));
+  if (rc) set_error("pnfft_gb300_sort_nodes: device allocation failed");
+  return rc;
+}
+
+int engine_node_index(pnfft_plan p, int64_t M, const double *x, int interlaced, long long *u) {
+  if (ensure_dev(p)) return -1;
+  cudaStream_t s = p->dev->stream;
+  if (M <= 0) return 0;
+  double *dx = nullptr;
+  long long *du = nullptr;
+  PG_CUDA(cudaMallocAsync(&dx, sizeof(double) * 3 * M, s));
+  PG_CUDA(cudaMallocAsync(&du, sizeof(long long) * 3 * M, s));
+  PG_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * 3 * M, cudaMemcpyHostToDevice, s));
+  int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
+  launch_node_index(dx, M, n, p->m, interlaced, du, s);
+  PG_CUDA(cudaMemcpyAsync(u, du, sizeof(long long) * 3 * M, cudaMemcpyDeviceToHost, s));
+  cudaFreeAsync(dx, s);
+  cudaFreeAsync(du, s);
+  PG_CUDA(cudaStreamSynchronize(s));
+  return 0;
+}
+
+}  // namespace pg

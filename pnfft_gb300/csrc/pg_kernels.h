@@ -1,0 +1,100 @@
+// pg_kernels.h -- argument blocks and launchers of the device kernels.
+// Included by the .cu files and by the host engine; no CUDA types appear in
+// the launcher signatures except cudaStream_t.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pg {
+
+// Window description shared by the convolution kernels.
+struct WindowArgs {
+  int kind;           // pg::WindowKind
+  int m, cut;         // cutoff = 2m+1
+  int n[3];           // oversampled grid
+  double b[3];        // shape parameters
+  int intpol_order;   // -1: evaluate directly; 0..3: tabulated (PNFFT_PRE_*_PSI)
+  int intpol_K;       // samples per grid cell of the tables
+  const void *tab[3][3];  // [derivative][axis], element type = compute precision
+};
+
+// Node binning onto grid tiles (one tile = T0 x T1 x T2 cells of lowest
+// stencil index).  A sub-problem is a run of at most `sub_max` nodes of one
+// tile; one CTA handles one sub-problem.
+struct Binning {
+  int T[3], ntile[3];
+  int ntiles, sub_max, max_subs;
+  int *key;        // [M] tile of each node
+  int *perm;       // [M] nodes sorted by tile
+  int *count;      // [ntiles]
+  int *start;      // [ntiles]
+  int *cursor;     // [ntiles]
+  int *nsub_tile;  // [ntiles]
+  int *sub_off;    // [ntiles]
+  int *sub_tile;   // [max_subs]
+  int *sub_first;  // [max_subs]
+  int *sub_cnt;    // [max_subs]
+  int *nsub;       // [1]
+};
+
+// One convolution (B or B^T) launch.
+struct ConvArgs {
+  WindowArgs w;
+  int use_il, il;   // interlacing: 0.5 scale / shifted pass
+  int real_only;    // read only the real parts of the grid (c2r and the
+                    // c2c + PNFFT_PRE_QUAD_PSI behaviour of the reference)
+  int real_io;      // node arrays are real (c2r) instead of complex
+  int64_t M;
+  const double *x;  // [M][3]
+  void *grid;       // n0*n1*n2 complex in compute precision, natural order
+  // node arrays (double, complex interleaved unless real_io), element ind = j*stride + offset
+  const double *f_in, *grad_in;
+  double *f_out, *grad_out, *hess_out;
+  int64_t offset, stride;
+  Binning bin;
+};
+
+// Launchers (conv.cu).  `fp32` selects the FP32-mixed kernels.  `mode` is a
+// bit set of 1 = f, 2 = grad, 4 = hessian (interp) / 1 = f, 2 = grad (spread).
+void bin_nodes(const ConvArgs &a, cudaStream_t s);
+void launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
+void launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
+void choose_tiles(int cut, bool fp32, const int *n, int *T);
+size_t conv_smem_bytes(const int *T, int cut, bool fp32, bool spread);
+
+// Deconvolution (deconv.cu).
+struct DeconvArgs {
+  int N[3], n[3];
+  int64_t Nl[3], ks[3];  // stored block of f_hat (c2r: Nl2 = N2/2+1)
+  int transposed, c2r;
+  const double *inv[3];  // inv_phi_hat per axis for k = ks..ks+Nl-1
+  int interlaced;
+  int ik;                // 0 none, 1 gradient component ik_dim, 2 Hessian component ik_dim
+  int ik_dim;
+  const double *fhat_in; // trafo: f_hat (complex double)
+  double *fhat_out;      // adjoint: accumulated f_hat
+  void *grid;            // n0*n1*n2 complex, compute precision
+};
+void launch_deconv_pad(const DeconvArgs &a, bool fp32, cudaStream_t s);
+void launch_deconv_crop_acc(const DeconvArgs &a, bool fp32, cudaStream_t s);
+
+// Verification helpers and the direct NDFT (sort.cu, ndft.cu).
+void launch_node_index(const double *x, int64_t M, const int *n, int m, int il, long long *u, cudaStream_t s);
+int radix_sort_nodes(const double *x, int64_t M, const int *n, int m, long long *pairs_dev, cudaStream_t s);
+
+struct NdftArgs {
+  int N[3];
+  int64_t Nl[3], ks[3];
+  int transposed, c2r;
+  int64_t M;
+  const double *x;
+  const double *fhat;  // complex
+  double *f, *grad, *hess;
+  const double *f_in, *grad_in;
+  double *fhat_out;
+  unsigned cflags;
+};
+void launch_ndft_trafo(const NdftArgs &a, cudaStream_t s);
+void launch_ndft_adj(const NdftArgs &a, cudaStream_t s);
+
+}  // namespace pg

@@ -1,0 +1,240 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+FP64: every transform variant agrees with the oracle's restatement of the
+reference on the same inputs to 1e-12 relative l2 (spec bar); node
+indices and the PNFFT_SORT_NODES permutation are bit-exact.
+FP32-mixed: within 2e-6 relative l2 of the FP64 NDFT at m = 6.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+WINDOWS = {
+    "kaiser_bessel": 0,
+    "gaussian": 1 << 13,
+    "bspline": 1 << 14,
+    "sinc_power": 1 << 15,
+    "bessel_i0": 1 << 16,
+    "gaussian_t": (1 << 17) | (1 << 13),
+}
+FP64_TOL = 1e-12
+
+
+def rel(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    d = np.linalg.norm((a - b).ravel())
+    nb = np.linalg.norm(b.ravel())
+    return d / nb if nb > 0 else d
+
+
+def case(N, M, seed, c2r=False, local_N=None):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    size = int(np.prod(local_N or N))
+    fh = rng.standard_normal(size) + 1j * rng.standard_normal(size)
+    if c2r:
+        f = rng.standard_normal(M)
+        g = rng.standard_normal((M, 3))
+    else:
+        f = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+        g = rng.standard_normal((M, 3)) + 1j * rng.standard_normal((M, 3))
+    return x, fh, f, g
+
+
+@pytest.fixture(scope="module")
+def gpu(lib):
+    if lib.device_count() == 0:
+        pytest.fail("no CUDA device visible for a -m gpu test")
+    return lib
+
+
+CF_ALL = 1 | 2 | 4
+
+
+@pytest.mark.parametrize("win", list(WINDOWS))
+def test_fp64_all_windows(gpu, oracle, win):
+    N, M = (16, 12, 20), 700
+    x, fh, f, g = case(N, M, 1)
+    p = gpu.Plan(N, m=4, flags=WINDOWS[win])
+    o = oracle.OraclePlan(N, m=4, flags=WINDOWS[win])
+    a = p.trafo(x, fh, CF_ALL)
+    b = o.trafo(x, fh, CF_ALL)
+    for u, v in zip(a, b):
+        assert rel(u, v) < FP64_TOL
+    fa = p.adj(x, f, g, 1 | 2)
+    fb = o.adj(x, f, g, 1 | 2)
+    assert rel(fa, fb) < FP64_TOL
+
+
+@pytest.mark.parametrize("mode", ["plain_m6", "interlaced", "diff_ik", "cub", "const", "quad_real_only",
+                                  "transposed", "sigma_1p5", "ik_interlaced", "fast_gaussian"])
+def test_fp64_modes(gpu, oracle, mode):
+    N, m, n = (16, 16, 16), 6, None
+    flags = {"plain_m6": 0, "interlaced": gpu.INTERLACED, "diff_ik": gpu.DIFF_IK, "cub": gpu.PRE_CUB_PSI,
+             "const": gpu.PRE_CONST_PSI, "quad_real_only": gpu.PRE_QUAD_PSI, "transposed": gpu.TRANSPOSED_F_HAT,
+             "sigma_1p5": 0, "ik_interlaced": gpu.DIFF_IK | gpu.INTERLACED,
+             "fast_gaussian": gpu.WINDOW_GAUSSIAN | gpu.FAST_GAUSSIAN}[mode]
+    if mode == "sigma_1p5":
+        N, n = (16, 8, 12), (24, 12, 18)
+    x, fh, f, g = case(N, 500, 2)
+    p = gpu.Plan(N, n, m=m, flags=flags)
+    o = oracle.OraclePlan(N, n, m=m, flags=flags)
+    a = p.trafo(x, fh, CF_ALL)
+    b = o.trafo(x, fh, CF_ALL)
+    for u, v in zip(a, b):
+        assert rel(u, v) < FP64_TOL, mode
+    fa = p.adj(x, f, g, 1 | 2)
+    fb = o.adj(x, f, g, 1 | 2)
+    assert rel(fa, fb) < FP64_TOL
+
+
+@pytest.mark.parametrize("m", [1, 2, 3, 5, 7, 8, 10])
+def test_fp64_cutoffs(gpu, oracle, m):
+    N = (8, 8, 12)
+    x, fh, f, g = case(N, 300, 3)
+    p = gpu.Plan(N, m=m)
+    o = oracle.OraclePlan(N, m=m)
+    a = p.trafo(x, fh, 1 | 2)
+    b = o.trafo(x, fh, 1 | 2)
+    assert rel(a[0], b[0]) < FP64_TOL and rel(a[1], b[1]) < FP64_TOL
+    assert rel(p.adj(x, f, g, 1 | 2), o.adj(x, f, g, 1 | 2)) < FP64_TOL
+
+
+@pytest.mark.parametrize("win", ["kaiser_bessel", "gaussian", "bspline"])
+def test_fp64_c2r(gpu, oracle, win):
+    N = (8, 12, 16)
+    p = gpu.Plan(N, m=5, flags=WINDOWS[win], c2r=True)
+    o = oracle.OraclePlan(N, m=5, flags=WINDOWS[win], c2r=True)
+    x, fh, f, g = case(N, 400, 4, c2r=True, local_N=p.local_N)
+    a = p.trafo(x, fh, CF_ALL)
+    b = o.trafo(x, fh, CF_ALL)
+    for u, v in zip(a, b):
+        assert rel(u, v) < FP64_TOL
+    assert rel(p.adj(x, f, g, 1 | 2), o.adj(x, f, g, 1 | 2)) < FP64_TOL
+
+
+def test_direct_ndft_on_gpu(gpu, oracle):
+    N = (8, 10, 12)
+    x, fh, f, g = case(N, 200, 5)
+    for flags in (0, gpu.TRANSPOSED_F_HAT):
+        p = gpu.Plan(N, m=3, flags=flags)
+        o = oracle.OraclePlan(N, m=3, flags=flags)
+        a = p.trafo(x, fh, CF_ALL | gpu.COMPUTE_DIRECT)
+        b = o.trafo(x, fh, CF_ALL | gpu.COMPUTE_DIRECT)
+        for u, v in zip(a, b):
+            assert rel(u, v) < 1e-12
+        assert rel(p.adj(x, f, g, 3 | gpu.COMPUTE_DIRECT), o.adj(x, f, g, 3 | gpu.COMPUTE_DIRECT)) < 1e-12
+    pr = gpu.Plan(N, m=3, c2r=True)
+    orr = oracle.OraclePlan(N, m=3, c2r=True)
+    x, fh, f, g = case(N, 200, 6, c2r=True, local_N=pr.local_N)
+    a = pr.trafo(x, fh, CF_ALL | gpu.COMPUTE_DIRECT)
+    b = orr.trafo(x, fh, CF_ALL | gpu.COMPUTE_DIRECT)
+    for u, v in zip(a, b):
+        assert rel(u, v) < 1e-12
+
+
+def test_check_vs_pfft_identity_gpu(gpu):
+    N = (16, 16, 16)
+    k = [np.arange(-n // 2, n // 2) for n in N]
+    K0, K1, K2 = np.meshgrid(*k, indexing="ij")
+    x = np.stack([K0.ravel() / N[0], K1.ravel() / N[1], K2.ravel() / N[2]], 1)
+    g = np.arange(int(np.prod(N)))
+    fh = 1000.0 / (2 * g + 1) + 1j * 1000.0 / (2 * g + 2)
+    for prec, tol in (("fp64", 1e-10), ("fp32", 1e-6)):
+        p = gpu.Plan(N, m=6, precision=prec)
+        f, _, _ = p.trafo(x, fh)
+        back = p.adj(x, f) / np.prod(N)
+        assert np.abs(back - fh).max() / np.abs(fh).sum() < tol, prec
+
+
+def test_node_index_and_sort_bitexact(gpu, oracle):
+    rng = np.random.default_rng(9)
+    N, n, m = (16, 16, 16), (32, 48, 40), 4
+    x = rng.uniform(-0.5, 0.5, (20000, 3))
+    # edge nodes: the interval ends, grid points, one ulp around grid points
+    edge = np.array([-0.5, 0.0, 0.5 - 2 ** -53, 1 / 32, -1 / 32, 15 / 32, -15 / 32, 3 / 48, 7 / 40])
+    edge = np.concatenate([edge, np.nextafter(edge, 1), np.nextafter(edge, -1)])
+    edge = edge[(edge >= -0.5) & (edge < 0.5)]
+    x[: edge.size * 3].reshape(-1, 3)[:] = 0
+    for t in range(3):
+        x[t * edge.size:(t + 1) * edge.size, t] = edge
+    x[5000:6000] = x[17]
+    p = gpu.Plan(N, n, m=m)
+    o = oracle.OraclePlan(N, n, m=m)
+    for il in (0, 1):
+        np.testing.assert_array_equal(p.node_index(x, il), o.node_index(x, il)[0])
+    np.testing.assert_array_equal(p.sort_nodes(x), o.sort_nodes(x))
+
+
+def test_fp32_mixed_vs_ndft(gpu, oracle):
+    N = (32, 32, 32)
+    M = 4096
+    rng = np.random.default_rng(12)
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    k = [np.arange(-n // 2, n // 2) for n in N]
+    K = np.stack(np.meshgrid(*k, indexing="ij"), -1).reshape(-1, 3)
+    fh = (rng.standard_normal(K.shape[0]) + 1j * rng.standard_normal(K.shape[0])) / (1 + (K ** 2).sum(1))
+    p = gpu.Plan(N, m=6, precision="fp32")
+    o = oracle.OraclePlan(N, m=6)
+    sub = slice(0, 512)
+    f, g, _ = p.trafo(x, fh, 1 | 2)
+    fd, gd, _ = o.trafo(x[sub], fh, 1 | 2 | gpu.COMPUTE_DIRECT)
+    assert rel(f[sub], fd) < 2e-6
+    assert rel(g[sub], gd) < 2e-6
+    fv = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    a = p.adj(x, fv)
+    ad = o.adj(x, fv, None, 1 | gpu.COMPUTE_DIRECT)
+    assert rel(a, ad) < 2e-6
+
+
+def test_accumulated_and_empty(gpu, oracle):
+    N = (8, 8, 8)
+    x, fh, f, g = case(N, 100, 13)
+    p = gpu.Plan(N, m=3)
+    o = oracle.OraclePlan(N, m=3)
+    f0 = np.arange(100) * (1 + 1j)
+    fa, _, _ = p.trafo(x, fh, 1 | gpu.COMPUTE_ACCUMULATED, f=f0.copy())
+    fb, _, _ = o.trafo(x, fh, 1 | gpu.COMPUTE_ACCUMULATED, f=f0.copy())
+    assert rel(fa, fb) < FP64_TOL
+    fh0 = np.ones(512, complex)
+    a = p.adj(x, f, None, 1 | gpu.COMPUTE_ACCUMULATED, f_hat=fh0.copy())
+    b = o.adj(x, f, None, 1 | gpu.COMPUTE_ACCUMULATED, f_hat=fh0.copy())
+    assert rel(a, b) < FP64_TOL
+    # no nodes: trafo returns nothing, adj returns zeros
+    e = np.zeros((0, 3))
+    fe, _, _ = p.trafo(e, fh)
+    assert fe.size == 0
+    assert np.abs(p.adj(e, np.zeros(0, complex))).max() == 0.0
+
+
+def test_clustered_nodes_large_bins(gpu, oracle):
+    # many nodes in one grid tile exercise the sub-problem split of the binning
+    N = (16, 16, 16)
+    rng = np.random.default_rng(14)
+    x = np.concatenate([rng.uniform(-0.5, 0.5, (500, 3)), 0.2 + 0.002 * rng.standard_normal((5000, 3))])
+    fh = rng.standard_normal(4096) + 1j * rng.standard_normal(4096)
+    f = rng.standard_normal(x.shape[0]) + 0j
+    for prec, tol in (("fp64", FP64_TOL), ("fp32", 2e-6)):
+        p = gpu.Plan(N, m=5, precision=prec)
+        o = oracle.OraclePlan(N, m=5)
+        assert rel(p.trafo(x, fh)[0], o.trafo(x, fh)[0]) < tol
+        assert rel(p.adj(x, f), o.adj(x, f)) < tol
+
+
+def test_zero_copy_device_api_matches_host(gpu):
+    torch = pytest.importorskip("torch")
+    N = (16, 16, 16)
+    x, fh, f, g = case(N, 1000, 15)
+    p = gpu.Plan(N, m=6, precision="fp32")
+    fa, ga, _ = p.trafo(x, fh, 1 | 2)
+    aa = p.adj(x, f, None, 1)
+    q = gpu.Plan(N, m=6, precision="fp32")
+    xd = torch.tensor(x, device="cuda")
+    fhd = torch.tensor(fh, device="cuda")
+    fd, gd, _ = q.trafo_device(xd, fhd, 1 | 2)
+    ad = q.adj_device(xd, torch.tensor(f, device="cuda"))
+    torch.cuda.synchronize()
+    assert rel(fd.cpu().numpy(), fa) < 1e-6
+    assert rel(gd.cpu().numpy(), ga) < 1e-6
+    assert rel(ad.cpu().numpy(), aa) < 1e-6
