@@ -70,7 +70,9 @@ int pnfft_gb300_synchronize(pnfft_plan ths);
  *    order, pairs[2p+1] = its original index (stable, bit-exact with the
  *    reference's radix sort, kernel/ndft-parallel.c:2121-2159);
  *  - the lowest grid index floor(n_t x_t) - m of every node (with the
- *    interlacing shift when interlaced != 0), kernel/ndft-parallel.c:2165-2174. */
+ *    interlacing shift when interlaced != 0), kernel/ndft-parallel.c:2165-2174,
+ *    evaluated the way the plan's binning evaluates it (FP64 arithmetic, or the
+ *    integer-only form of FP32-mixed plans). */
 int pnfft_gb300_sort_nodes(pnfft_plan ths, ptrdiff_t M, const double *x, long long *pairs);
 int pnfft_gb300_node_index(pnfft_plan ths, ptrdiff_t M, const double *x, int interlaced, long long *u);
 

@@ -41,6 +41,14 @@ class PnfftError(RuntimeError):
     pass
 
 
+def _stream_handle(stream):
+    """cudaStream_t of a torch stream; torch's default stream (handle 0) is the
+    legacy default stream, passed as cudaStreamLegacy (0x1) because a NULL
+    stream selects the plan's own stream."""
+    h = stream.cuda_stream
+    return h if h else 0x1
+
+
 def _check(rc=0, what="pnfft"):
     msg = last_error()
     if rc != 0 or msg:
@@ -244,7 +252,7 @@ class Plan:
             grad = torch.empty(M, 3, dtype=dt, device=x.device)
         if compute_flags & COMPUTE_HESSIAN_F and hess is None:
             hess = torch.empty(M, 6, dtype=dt, device=x.device)
-        s = (stream or torch.cuda.current_stream(x.device)).cuda_stream
+        s = _stream_handle(stream or torch.cuda.current_stream(x.device))
         nd = self._bind_device(x, f, grad, hess, f_hat, s)
         L = load()
         if fixed_nodes:
@@ -260,7 +268,7 @@ class Plan:
         import torch
         if f_hat is None:
             f_hat = torch.empty(int(np.prod(self.local_N)), dtype=torch.complex128, device=x.device)
-        s = (stream or torch.cuda.current_stream(x.device)).cuda_stream
+        s = _stream_handle(stream or torch.cuda.current_stream(x.device))
         nd = self._bind_device(x, f, grad, None, f_hat, s)
         L = load()
         if fixed_nodes:

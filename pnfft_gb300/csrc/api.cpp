@@ -288,6 +288,20 @@ static unsigned extract_pfft_opt_flags(unsigned f) {  // api/api-guru.c:168-190
   return r;
 }
 
+// The radial windows grow like exp(b m): Kaiser-Bessel and Bessel-I0 with
+// b m >= 80 (m >= 17 at oversampling 2) overflow FP32, so FP32-mixed plans
+// refuse them.
+static bool fp32_window_in_range(const pnfft_plan p) {
+  if (p->window != WIN_KAISER_BESSEL && p->window != WIN_BESSEL_I0) return true;
+  for (int t = 0; t < 3; t++)
+    if (p->b[t] * (double)p->m >= 80.0) {
+      set_error("FP32-mixed precision: the %s window with m=%d overflows FP32 (b*m=%.1f >= 80); use FP64",
+                p->window == WIN_KAISER_BESSEL ? "Kaiser-Bessel" : "Bessel-I0", p->m, p->b[t] * (double)p->m);
+      return false;
+    }
+  return true;
+}
+
 static pnfft_plan init_guru_internal(int d, const ptrdiff_t *N, const ptrdiff_t *n, const double *x_max, int m,
                                      int c2r, unsigned pnfft_flags, unsigned pfft_flags) {
   if (d != 3) {
@@ -357,6 +371,10 @@ static pnfft_plan init_guru_internal(int d, const ptrdiff_t *N, const ptrdiff_t 
     }
   }
   p->precision = (pnfft_flags & PNFFT_GB300_FP32) ? PNFFT_GB300_FP32_MIXED : PNFFT_GB300_FP64;
+  if (p->precision == PNFFT_GB300_FP32_MIXED && !fp32_window_in_range(p)) {
+    delete p;
+    return nullptr;
+  }
   p->uid = g_uid.fetch_add(1);
   if (pnfft_flags & PNFFT_MALLOC_F_HAT) {
     p->f_hat = pnfft_malloc(sizeof(double) * 2 * (size_t)p->local_N_total);
@@ -862,6 +880,7 @@ extern "C" int pnfft_gb300_set_precision(pnfft_plan ths, int precision) {
     set_error("pnfft_gb300_set_precision: unknown precision %d", precision);
     return -1;
   }
+  if (precision == PNFFT_GB300_FP32_MIXED && !fp32_window_in_range(ths)) return -1;
   if (ths->precision != precision) {
     engine_sync(ths);
     ths->precision = precision;

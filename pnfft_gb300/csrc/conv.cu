@@ -22,6 +22,7 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 
+#include "pg_index.cuh"
 #include "pg_kernels.h"
 #include "pg_math.cuh"
 
@@ -67,87 +68,176 @@ __device__ __forceinline__ AxisPos axis_pos(double x, int n, int m, int il) {
 }
 
 // window values of one node: ws[der*3*cut + t*cut + s]
-template <typename T>
-__device__ __forceinline__ void warp_windows(const WindowArgs &w, const double *dist, int nder, T *ws, int lane) {
-  const int cut = w.cut;
-  for (int e = lane; e < 3 * cut; e += 32) {
-    int t = e / cut, s = e - t * cut;
-    T out[3] = {(T)0, (T)0, (T)0};
-    if (w.intpol_order >= 0) {
-      double dK = dist[t] * (double)w.intpol_K;
-      long long k = (long long)floor(dK);
-      T dk = (T)(dK - (double)k);
-      size_t base = ((size_t)k * cut + s) * (size_t)(w.intpol_order + 1);
-      for (int d = 0; d <= nder; d++) out[d] = intpol<T>(w.intpol_order, (const T *)w.tab[d][t] + base, dk);
-    } else {
-      T y = (T)dist[t] + (T)(w.m - s);
-      T smd = (T)s - (T)dist[t];
-      window_eval<T>(w.kind, w.m, (T)w.n[t], (T)w.b[t], y, smd, nder, out);
-    }
-    ws[e] = out[0];
-    if (nder >= 1) ws[3 * cut + e] = out[1];
-    if (nder >= 2) ws[6 * cut + e] = out[2];
-  }
-}
-
 // ---------------------------------------------------------------------------
 // binning
+//
+// k_bin_keys computes, once per node, the lowest stencil index u (bit-exact)
+// and the fractional positions, writes the node record (unsorted) and counts
+// nodes per tile; a three-phase scan gives tile starts and the sub-problem
+// list; k_bin_scatter moves perm and records into tile order.
+// For the FP32-mixed form without interlacing, floor(fl(n x)) is evaluated
+// with integer arithmetic on the bits of x (the FP64 pipe of GB300 is slow):
+// the exact product n*M_x (<= 73 bits) is rounded to 53 bits with ties to
+// even -- which is fl(n x) -- and split into integer and fractional parts.
 // ---------------------------------------------------------------------------
-__global__ void k_bin_keys(const double *__restrict__ x, int64_t M, int n0, int n1, int n2, int m, int il, int T0,
-                           int T1, int T2, int nt1, int nt2, int *__restrict__ key, int *__restrict__ count) {
-  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= M) return;
-  AxisPos p0 = axis_pos(x[3 * j + 0], n0, m, il);
-  AxisPos p1 = axis_pos(x[3 * j + 1], n1, m, il);
-  AxisPos p2 = axis_pos(x[3 * j + 2], n2, m, il);
-  int tile = ((p0.u / T0) * nt1 + p1.u / T1) * nt2 + p2.u / T2;
-  key[j] = tile;
-  atomicAdd(&count[tile], 1);
+__device__ __forceinline__ void store_rec(void *rec, int64_t pos, const float *dist, int opk, float) {
+  ((float4 *)rec)[pos] = make_float4(dist[0], dist[1], dist[2], __int_as_float(opk));
+}
+__device__ __forceinline__ void store_rec(void *rec, int64_t pos, const double *dist, int opk, double) {
+  ((double4 *)rec)[pos] = make_double4(dist[0], dist[1], dist[2], __longlong_as_double((long long)opk));
 }
 
-// exclusive scans of count and of the number of sub-problems per tile (one CTA)
-__global__ void __launch_bounds__(1024) k_bin_scan(Binning b) {
-  __shared__ int s_a[1024], s_b[1024];
-  const int tid = threadIdx.x, nt = b.ntiles;
-  const int chunk = (nt + 1023) / 1024;
-  const int lo = min(nt, tid * chunk), hi = min(nt, lo + chunk);
+template <typename T>
+__global__ void k_bin_keys(const double *__restrict__ x, int64_t M, int n0, int n1, int n2, int m, int il,
+                           Binning b, void *__restrict__ rec_unsorted) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= M) return;
+  const int nn[3] = {n0, n1, n2};
+  T dist[3];
+  int u[3];
+  for (int d = 0; d < 3; d++) {
+    if (sizeof(T) == 4 && !il) {
+      long long fnx;
+      float fr;
+      nx_exact(x[3 * j + d], nn[d], &fnx, &fr);
+      long long w = (fnx - m) % nn[d];
+      if (w < 0) w += nn[d];
+      u[d] = (int)w;
+      dist[d] = (T)fr;
+    } else {
+      AxisPos p = axis_pos(x[3 * j + d], nn[d], m, il);
+      u[d] = p.u;
+      dist[d] = (T)p.dist;
+    }
+  }
+  const int t0 = u[0] / b.T[0], t1 = u[1] / b.T[1], t2 = u[2] / b.T[2];
+  const int tile = (t0 * b.ntile[1] + t1) * b.ntile[2] + t2;
+  const int opk = (u[0] - t0 * b.T[0]) | ((u[1] - t1 * b.T[1]) << 8) | ((u[2] - t2 * b.T[2]) << 16);
+  b.key[j] = tile;
+  store_rec(rec_unsorted, j, dist, opk, T(0));
+  atomicAdd(&b.count[tile], 1);
+}
+
+// three-phase exclusive scan of the tile counts and sub-problem counts
+constexpr int kScanBlock = 2048;
+
+__global__ void __launch_bounds__(256) k_bin_scan_a(Binning b, int *bsum) {
+  __shared__ int ra[256], rb[256];
+  const int lo = blockIdx.x * kScanBlock;
   int sa = 0, sb = 0;
-  for (int i = lo; i < hi; i++) {
+  for (int i = lo + threadIdx.x; i < min(b.ntiles, lo + kScanBlock); i += 256) {
     int c = b.count[i];
     sa += c;
     sb += (c + b.sub_max - 1) / b.sub_max;
   }
-  s_a[tid] = sa;
-  s_b[tid] = sb;
+  ra[threadIdx.x] = sa;
+  rb[threadIdx.x] = sb;
   __syncthreads();
-  for (int off = 1; off < 1024; off <<= 1) {
-    int va = (tid >= off) ? s_a[tid - off] : 0;
-    int vb = (tid >= off) ? s_b[tid - off] : 0;
-    __syncthreads();
-    s_a[tid] += va;
-    s_b[tid] += vb;
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) {
+      ra[threadIdx.x] += ra[threadIdx.x + o];
+      rb[threadIdx.x] += rb[threadIdx.x + o];
+    }
     __syncthreads();
   }
-  int pa = s_a[tid] - sa, pb = s_b[tid] - sb;
-  for (int i = lo; i < hi; i++) {
-    int c = b.count[i];
-    int ns = (c + b.sub_max - 1) / b.sub_max;
-    b.start[i] = pa;
-    b.cursor[i] = 0;
-    b.nsub_tile[i] = ns;
-    b.sub_off[i] = pb;
-    pa += c;
-    pb += ns;
+  if (threadIdx.x == 0) {
+    bsum[2 * blockIdx.x] = ra[0];
+    bsum[2 * blockIdx.x + 1] = rb[0];
   }
-  if (tid == 1023) *b.nsub = s_b[1023];
 }
 
-__global__ void k_bin_scatter(int64_t M, Binning b) {
+__global__ void __launch_bounds__(1024) k_bin_scan_b(Binning b, int *bsum, int nblk) {
+  __shared__ int sa[1024], sb[1024];
+  const int tid = threadIdx.x;
+  const int chunk = (nblk + 1023) / 1024;
+  const int lo = min(nblk, tid * chunk), hi = min(nblk, lo + chunk);
+  int a = 0, c = 0;
+  for (int i = lo; i < hi; i++) {
+    a += bsum[2 * i];
+    c += bsum[2 * i + 1];
+  }
+  sa[tid] = a;
+  sb[tid] = c;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    int va = (tid >= off) ? sa[tid - off] : 0, vb = (tid >= off) ? sb[tid - off] : 0;
+    __syncthreads();
+    sa[tid] += va;
+    sb[tid] += vb;
+    __syncthreads();
+  }
+  int pa = sa[tid] - a, pb = sb[tid] - c;
+  for (int i = lo; i < hi; i++) {
+    int x0 = bsum[2 * i], x1 = bsum[2 * i + 1];
+    bsum[2 * i] = pa;
+    bsum[2 * i + 1] = pb;
+    pa += x0;
+    pb += x1;
+  }
+  if (tid == 1023) *b.nsub = sb[1023];
+}
+
+__global__ void __launch_bounds__(256) k_bin_scan_c(Binning b, const int *bsum) {
+  __shared__ int ca[kScanBlock], cb[kScanBlock];
+  __shared__ int wa[8], wb[8];
+  const int lo = blockIdx.x * kScanBlock, tid = threadIdx.x;
+  const int n = min(kScanBlock, b.ntiles - lo);
+  for (int i = tid; i < kScanBlock; i += 256) {
+    int c = (i < n) ? b.count[lo + i] : 0;
+    ca[i] = c;
+    cb[i] = (c + b.sub_max - 1) / b.sub_max;
+  }
+  __syncthreads();
+  // each thread scans 8 consecutive entries, then a warp-level scan of the thread sums
+  const int k0 = tid * 8;
+  int ta = 0, tb = 0;
+  for (int k = 0; k < 8; k++) {
+    ta += ca[k0 + k];
+    tb += cb[k0 + k];
+  }
+  const int lane = tid & 31, w = tid >> 5;
+  int xa = ta, xb = tb;
+  for (int o = 1; o < 32; o <<= 1) {
+    int ya = __shfl_up_sync(0xffffffffu, xa, o), yb = __shfl_up_sync(0xffffffffu, xb, o);
+    if (lane >= o) {
+      xa += ya;
+      xb += yb;
+    }
+  }
+  if (lane == 31) {
+    wa[w] = xa;
+    wb[w] = xb;
+  }
+  __syncthreads();
+  int oa = bsum[2 * blockIdx.x], ob = bsum[2 * blockIdx.x + 1];
+  for (int v = 0; v < w; v++) {
+    oa += wa[v];
+    ob += wb[v];
+  }
+  oa += xa - ta;
+  ob += xb - tb;
+  for (int k = 0; k < 8; k++) {
+    const int i = k0 + k;
+    if (i < n) {
+      b.start[lo + i] = oa;
+      b.cursor[lo + i] = 0;
+      b.nsub_tile[lo + i] = cb[i];
+      b.sub_off[lo + i] = ob;
+    }
+    oa += ca[i];
+    ob += cb[i];
+  }
+}
+
+template <typename T>
+__global__ void k_bin_scatter(int64_t M, Binning b, const void *__restrict__ rec_unsorted) {
   int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= M) return;
-  int t = b.key[j];
-  int pos = b.start[t] + atomicAdd(&b.cursor[t], 1);
+  const int t = b.key[j];
+  const int pos = b.start[t] + atomicAdd(&b.cursor[t], 1);
   b.perm[pos] = (int)j;
+  if (sizeof(T) == 4) ((float4 *)b.rec)[pos] = ((const float4 *)rec_unsorted)[j];
+  else ((double4 *)b.rec)[pos] = ((const double4 *)rec_unsorted)[j];
 }
 
 __global__ void k_bin_subs(Binning b) {
@@ -161,20 +251,24 @@ __global__ void k_bin_subs(Binning b) {
   }
 }
 
-void bin_nodes(const ConvArgs &a, cudaStream_t s) {
+void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s) {
   const Binning &b = a.bin;
   cudaMemsetAsync(b.count, 0, sizeof(int) * b.ntiles, s);
+  const int th = 256;
+  const unsigned bl = (unsigned)((a.M + th - 1) / th);
   if (a.M > 0) {
-    int th = 256;
-    int64_t bl = (a.M + th - 1) / th;
-    k_bin_keys<<<(unsigned)bl, th, 0, s>>>(a.x, a.M, a.w.n[0], a.w.n[1], a.w.n[2], a.w.m, a.il, b.T[0], b.T[1], b.T[2],
-                                            b.ntile[1], b.ntile[2], b.key, b.count);
+    if (fp32)
+      k_bin_keys<float><<<bl, th, 0, s>>>(a.x, a.M, a.w.n[0], a.w.n[1], a.w.n[2], a.w.m, a.il, b, b.rec_tmp);
+    else
+      k_bin_keys<double><<<bl, th, 0, s>>>(a.x, a.M, a.w.n[0], a.w.n[1], a.w.n[2], a.w.m, a.il, b, b.rec_tmp);
   }
-  k_bin_scan<<<1, 1024, 0, s>>>(b);
+  const int nblk = (b.ntiles + kScanBlock - 1) / kScanBlock;
+  k_bin_scan_a<<<nblk, 256, 0, s>>>(b, b.bsum);
+  k_bin_scan_b<<<1, 1024, 0, s>>>(b, b.bsum, nblk);
+  k_bin_scan_c<<<nblk, 256, 0, s>>>(b, b.bsum);
   if (a.M > 0) {
-    int th = 256;
-    int64_t bl = (a.M + th - 1) / th;
-    k_bin_scatter<<<(unsigned)bl, th, 0, s>>>(a.M, b);
+    if (fp32) k_bin_scatter<float><<<bl, th, 0, s>>>(a.M, b, b.rec_tmp);
+    else k_bin_scatter<double><<<bl, th, 0, s>>>(a.M, b, b.rec_tmp);
   }
   k_bin_subs<<<(b.ntiles + 255) / 256, 256, 0, s>>>(b);
 }
@@ -206,273 +300,491 @@ __device__ __forceinline__ void atomic_add_grid(double2 *p, double2 v) {
 }
 
 // ---------------------------------------------------------------------------
-// interpolation B, tiled (compile-time cutoff CUT <= 16)
+// shared helpers of the tiled kernels (8x8x8-cell tiles, compile-time cutoff)
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ void window_formula(const WindowArgs &w, int t, int s, float dist, int nder, float *out) {
+  window_eval_f(w.kind, w.m, w.wf[t], w.m - s, dist, nder, out);
+}
+__device__ __forceinline__ void window_formula(const WindowArgs &w, int t, int s, double dist, int nder,
+                                               double *out) {
+  window_eval<double>(w.kind, w.m, (double)w.n[t], w.b[t], dist + (double)(w.m - s), (double)s - dist, nder, out);
+}
+
+// psi (and derivatives up to nder) of stencil point s on axis t for a node at
+// fractional position dist, from the formula or the interpolation table
+template <typename T>
+__device__ __forceinline__ void window_point(const WindowArgs &w, int t, int s, T dist, int nder, T *out) {
+  if (w.intpol_order >= 0) {
+    T dK = dist * (T)w.intpol_K;
+    int k = (int)floor(dK);
+    T dk = dK - (T)k;
+    size_t base = ((size_t)k * w.cut + s) * (size_t)(w.intpol_order + 1);
+    for (int d = 0; d <= nder; d++) out[d] = intpol<T>(w.intpol_order, (const T *)w.tab[d][t] + base, dk);
+  } else {
+    window_formula(w, t, s, dist, nder, out);
+  }
+}
+
+__device__ __forceinline__ void unpack_corner(int pk, int *o) {
+  o[0] = pk & 0xff;
+  o[1] = (pk >> 8) & 0xff;
+  o[2] = (pk >> 16) & 0xff;
+}
+
+__device__ __forceinline__ void load_rec_raw(const void *rec, int pos, float *d, int *pk) {
+  float4 r = ((const float4 *)rec)[pos];
+  d[0] = r.x;
+  d[1] = r.y;
+  d[2] = r.z;
+  *pk = __float_as_int(r.w);
+}
+__device__ __forceinline__ void load_rec_raw(const void *rec, int pos, double *d, int *pk) {
+  double4 r = ((const double4 *)rec)[pos];
+  d[0] = r.x;
+  d[1] = r.y;
+  d[2] = r.z;
+  *pk = (int)__double_as_longlong(r.w);
+}
+
+// ---------------------------------------------------------------------------
+// interpolation B, tiled.  The CTA stages its tile's (8+2m)^3 region in
+// shared memory, then walks its nodes in batches: (1) all threads evaluate
+// the window values of the batch (3 x cutoff per node and derivative), (2)
+// one warp per node sums the 13^3 stencil -- lanes (row = lane/16, col =
+// lane%16) read two z-rows of 13 consecutive grid values per step, with the
+// x-window in registers -- and reduces with shuffles, (3) the batch's results
+// are converted and written by all threads.
+// ---------------------------------------------------------------------------
+template <typename T, int CUT, int MODE>
+struct InterpGeom {
+  static constexpr bool DF = (MODE & 1) != 0, DG = (MODE & 2) != 0, DH = (MODE & 4) != 0;
+  static constexpr int NDER = DH ? 2 : (DG ? 1 : 0);
+  static constexpr int R = 8 + CUT - 1, PL = R * R, VOL = R * R * R;
+  static constexpr int NV = 3 * CUT * (NDER + 1);
+  static constexpr int NC = (DF ? 1 : 0) + (DG ? 3 : 0) + (DH ? 6 : 0);
+  static constexpr int NBI = sizeof(T) == 4 ? 48 : 32;
+  static constexpr size_t SMEM = (size_t)VOL * 2 * sizeof(T) + (size_t)NBI * (NV + 2 * NC + 4) * sizeof(T) +
+                                 (size_t)NBI * 2 * sizeof(int);
+};
+
 template <typename T, int CUT, int MODE>
 __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
   typedef typename Cplx<T>::type C;
-  constexpr bool DF = (MODE & 1) != 0, DG = (MODE & 2) != 0, DH = (MODE & 4) != 0;
-  constexpr int NDER = DH ? 2 : (DG ? 1 : 0);
+  typedef InterpGeom<T, CUT, MODE> G;
+  constexpr bool DF = G::DF, DG = G::DG, DH = G::DH;
+  constexpr int NDER = G::NDER, R = G::R, PL = G::PL, VOL = G::VOL, NV = G::NV, NC = G::NC, NBI = G::NBI;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *reg = (C *)smem_raw;
+  T *s_w = (T *)(reg + VOL);     // [NBI][NV]
+  T *s_res = s_w + NBI * NV;     // [NBI][2*NC]
+  T *s_d = s_res + NBI * 2 * NC; // [NBI][4]
+  int *s_j = (int *)(s_d + NBI * 4);
+  int *s_o = s_j + NBI;
   const Binning &b = a.bin;
   const int sub = blockIdx.x;
   if (sub >= *b.nsub) return;
   const int tile = b.sub_tile[sub], first = b.sub_first[sub], cnt = b.sub_cnt[sub];
   int base[3];
   tile_base(b, tile, base);
-  const int R0 = b.T[0] + CUT - 1, R1 = b.T[1] + CUT - 1, R2 = b.T[2] + CUT - 1;
-  const int vol = R0 * R1 * R2;
-  C *reg = (C *)smem_raw;
-  T *wsall = (T *)(reg + vol);
   const int n0 = a.w.n[0], n1 = a.w.n[1], n2 = a.w.n[2];
+  const int tid = threadIdx.x;
   const C *grid = (const C *)a.grid;
-  for (int i = threadIdx.x; i < vol; i += blockDim.x) {
-    int c = i % R2, q = i / R2;
-    int bb = q % R1, aa = q / R1;
-    int g0 = (base[0] + aa) % n0, g1 = (base[1] + bb) % n1, g2 = (base[2] + c) % n2;
+  for (int i = tid; i < VOL; i += blockDim.x) {
+    int c = i % R, q = i / R;
+    int bb = q % R, aa = q / R;
+    int g0 = base[0] + aa, g1 = base[1] + bb, g2 = base[2] + c;
+    if (g0 >= n0) g0 %= n0;
+    if (g1 >= n1) g1 %= n1;
+    if (g2 >= n2) g2 %= n2;
     C v = grid[((size_t)g0 * n1 + g1) * n2 + g2];
     if (a.real_only) v.y = (T)0;
     reg[i] = v;
   }
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  T *ws = wsall + warp * (9 * CUT);
+  const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
   const int row = lane >> 4, col = lane & 15;
   const T scale = a.use_il ? (T)0.5 : (T)1;
-  for (int q = warp; q < cnt; q += nwarp) {
-    const int j = b.perm[first + q];
-    double dist[3];
-    int o[3];
-#pragma unroll
-    for (int t = 0; t < 3; t++) {
-      AxisPos p = axis_pos(a.x[3 * (int64_t)j + t], a.w.n[t], a.w.m, a.il);
-      dist[t] = p.dist;
-      o[t] = p.u - base[t];
+  for (int b0 = 0; b0 < cnt; b0 += NBI) {
+    const int nb = min(NBI, cnt - b0);
+    __syncthreads();  // region loaded / previous batch flushed
+    for (int i = tid; i < nb; i += blockDim.x) {
+      T d[3];
+      int pk;
+      load_rec_raw(b.rec, first + b0 + i, d, &pk);
+      s_d[4 * i] = d[0];
+      s_d[4 * i + 1] = d[1];
+      s_d[4 * i + 2] = d[2];
+      s_o[i] = pk;
+      s_j[i] = b.perm[first + b0 + i];
     }
-    warp_windows<T>(a.w, dist, NDER, ws, lane);
-    __syncwarp();
-    T px[CUT], dpx[CUT], ddpx[CUT];
-#pragma unroll
-    for (int l = 0; l < CUT; l++) {
-      px[l] = ws[l];
-      if (NDER >= 1) dpx[l] = ws[3 * CUT + l];
-      if (NDER >= 2) ddpx[l] = ws[6 * CUT + l];
+    __syncthreads();
+    for (int v = tid; v < nb * 3 * CUT; v += blockDim.x) {
+      const int i = v / (3 * CUT), e = v - i * 3 * CUT;
+      const int t = e / CUT, sidx = e - t * CUT;
+      T out[3];
+      window_point<T>(a.w, t, sidx, s_d[4 * i + t], NDER, out);
+      T *wv = s_w + i * NV;
+      wv[e] = out[0];
+      if (NDER >= 1) wv[3 * CUT + e] = out[1];
+      if (NDER >= 2) wv[6 * CUT + e] = out[2];
     }
-    // accumulators: f; grad x,y,z; hessian xx,xy,xz,yy,yz,zz
-    T af_r = 0, af_i = 0;
-    T ag_r[3] = {0, 0, 0}, ag_i[3] = {0, 0, 0};
-    T ah_r[6] = {0, 0, 0, 0, 0, 0}, ah_i[6] = {0, 0, 0, 0, 0, 0};
-    if (col < CUT) {
-      const T pz = ws[2 * CUT + col];
-      const T dz = (NDER >= 1) ? ws[3 * CUT + 2 * CUT + col] : (T)0;
-      const T ddz = (NDER >= 2) ? ws[6 * CUT + 2 * CUT + col] : (T)0;
-      for (int l1 = row; l1 < CUT; l1 += 2) {
-        const T py = ws[CUT + l1];
-        const T dy = (NDER >= 1) ? ws[3 * CUT + CUT + l1] : (T)0;
-        const T ddy = (NDER >= 2) ? ws[6 * CUT + CUT + l1] : (T)0;
-        const C *p = reg + ((size_t)o[0] * R1 + (o[1] + l1)) * R2 + (o[2] + col);
-        T s_r = 0, s_i = 0, sd_r = 0, sd_i = 0, sdd_r = 0, sdd_i = 0;
+    __syncthreads();
+    for (int i = warp; i < nb; i += nwarp) {
+      const T *wv = s_w + i * NV;
+      int o[3];
+      unpack_corner(s_o[i], o);
+      T px[CUT], dpx[CUT], ddpx[CUT];
 #pragma unroll
-        for (int l0 = 0; l0 < CUT; l0++) {
-          C g = p[(size_t)l0 * R1 * R2];
-          s_r += px[l0] * g.x;
-          s_i += px[l0] * g.y;
-          if (NDER >= 1) {
-            sd_r += dpx[l0] * g.x;
-            sd_i += dpx[l0] * g.y;
+      for (int l = 0; l < CUT; l++) {
+        px[l] = wv[l];
+        if (NDER >= 1) dpx[l] = wv[3 * CUT + l];
+        if (NDER >= 2) ddpx[l] = wv[6 * CUT + l];
+      }
+      T af_r = 0, af_i = 0;
+      T ag_r[3] = {0, 0, 0}, ag_i[3] = {0, 0, 0};
+      T ah_r[6] = {0, 0, 0, 0, 0, 0}, ah_i[6] = {0, 0, 0, 0, 0, 0};
+      if (col < CUT) {
+        const T pz = wv[2 * CUT + col];
+        const T dz = (NDER >= 1) ? wv[3 * CUT + 2 * CUT + col] : (T)0;
+        const T ddz = (NDER >= 2) ? wv[6 * CUT + 2 * CUT + col] : (T)0;
+        const C *pc = reg + (o[0] * R + o[1]) * R + (o[2] + col);
+#pragma unroll
+        for (int it = 0; it < (CUT + 1) / 2; it++) {
+          const int l1 = 2 * it + row;
+          if (l1 < CUT) {
+            const T py = wv[CUT + l1];
+            const T dy = (NDER >= 1) ? wv[3 * CUT + CUT + l1] : (T)0;
+            const T ddy = (NDER >= 2) ? wv[6 * CUT + CUT + l1] : (T)0;
+            const C *p = pc + l1 * R;
+            T s_r = 0, s_i = 0, sd_r = 0, sd_i = 0, sdd_r = 0, sdd_i = 0;
+#pragma unroll
+            for (int l0 = 0; l0 < CUT; l0++) {
+              const C g = p[l0 * PL];
+              s_r += px[l0] * g.x;
+              s_i += px[l0] * g.y;
+              if (NDER >= 1) {
+                sd_r += dpx[l0] * g.x;
+                sd_i += dpx[l0] * g.y;
+              }
+              if (NDER >= 2) {
+                sdd_r += ddpx[l0] * g.x;
+                sdd_i += ddpx[l0] * g.y;
+              }
+            }
+            const T wyz = py * pz;
+            if (DF) {
+              af_r += wyz * s_r;
+              af_i += wyz * s_i;
+            }
+            if (DG) {
+              ag_r[0] += wyz * sd_r;
+              ag_i[0] += wyz * sd_i;
+              ag_r[1] += dy * pz * s_r;
+              ag_i[1] += dy * pz * s_i;
+              ag_r[2] += py * dz * s_r;
+              ag_i[2] += py * dz * s_i;
+            }
+            if (DH) {
+              ah_r[0] += wyz * sdd_r;
+              ah_i[0] += wyz * sdd_i;
+              ah_r[1] += dy * pz * sd_r;
+              ah_i[1] += dy * pz * sd_i;
+              ah_r[2] += py * dz * sd_r;
+              ah_i[2] += py * dz * sd_i;
+              ah_r[3] += ddy * pz * s_r;
+              ah_i[3] += ddy * pz * s_i;
+              ah_r[4] += dy * dz * s_r;
+              ah_i[4] += dy * dz * s_i;
+              ah_r[5] += py * ddz * s_r;
+              ah_i[5] += py * ddz * s_i;
+            }
           }
-          if (NDER >= 2) {
-            sdd_r += ddpx[l0] * g.x;
-            sdd_i += ddpx[l0] * g.y;
-          }
-        }
-        const T wyz = py * pz;
-        if (DF) {
-          af_r += wyz * s_r;
-          af_i += wyz * s_i;
-        }
-        if (DG) {
-          ag_r[0] += wyz * sd_r;
-          ag_i[0] += wyz * sd_i;
-          ag_r[1] += dy * pz * s_r;
-          ag_i[1] += dy * pz * s_i;
-          ag_r[2] += py * dz * s_r;
-          ag_i[2] += py * dz * s_i;
-        }
-        if (DH) {
-          ah_r[0] += wyz * sdd_r;
-          ah_i[0] += wyz * sdd_i;
-          ah_r[1] += dy * pz * sd_r;
-          ah_i[1] += dy * pz * sd_i;
-          ah_r[2] += py * dz * sd_r;
-          ah_i[2] += py * dz * sd_i;
-          ah_r[3] += ddy * pz * s_r;
-          ah_i[3] += ddy * pz * s_i;
-          ah_r[4] += dy * dz * s_r;
-          ah_i[4] += dy * dz * s_i;
-          ah_r[5] += py * ddz * s_r;
-          ah_i[5] += py * ddz * s_i;
         }
       }
-    }
-    const int64_t ind = (int64_t)j * a.stride + a.offset;
-    if (DF) {
-      af_r = warp_sum(af_r);
-      af_i = warp_sum(af_i);
-      if (lane == 0) {
-        if (a.real_io) a.f_out[ind] += (double)(af_r * scale);
-        else {
-          a.f_out[2 * ind] += (double)(af_r * scale);
-          a.f_out[2 * ind + 1] += (double)(af_i * scale);
-        }
-      }
-    }
-    if (DG) {
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        T r = warp_sum(ag_r[c]), im = warp_sum(ag_i[c]);
+      T *res = s_res + i * 2 * NC;
+      int c = 0;
+      if (DF) {
+        T r = warp_sum(af_r), im = warp_sum(af_i);
         if (lane == 0) {
-          if (a.real_io) a.grad_out[3 * ind + c] += (double)(r * scale);
-          else {
-            a.grad_out[2 * (3 * ind + c)] += (double)(r * scale);
-            a.grad_out[2 * (3 * ind + c) + 1] += (double)(im * scale);
-          }
+          res[0] = r * scale;
+          res[1] = im * scale;
         }
+        c = 1;
       }
-    }
-    if (DH) {
+      if (DG) {
 #pragma unroll
-      for (int c = 0; c < 6; c++) {
-        T r = warp_sum(ah_r[c]), im = warp_sum(ah_i[c]);
-        if (lane == 0) {
-          if (a.real_io) a.hess_out[6 * ind + c] += (double)(r * scale);
-          else {
-            a.hess_out[2 * (6 * ind + c)] += (double)(r * scale);
-            a.hess_out[2 * (6 * ind + c) + 1] += (double)(im * scale);
+        for (int k = 0; k < 3; k++) {
+          T r = warp_sum(ag_r[k]), im = warp_sum(ag_i[k]);
+          if (lane == 0) {
+            res[2 * (c + k)] = r * scale;
+            res[2 * (c + k) + 1] = im * scale;
+          }
+        }
+      }
+      if (DH) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+          T r = warp_sum(ah_r[k]), im = warp_sum(ah_i[k]);
+          if (lane == 0) {
+            res[2 * k] = r * scale;
+            res[2 * k + 1] = im * scale;
           }
         }
       }
     }
-    __syncwarp();
+    __syncthreads();
+    // write the batch: one thread per (node, output component)
+    for (int v = tid; v < nb * NC; v += blockDim.x) {
+      const int i = v / NC, k = v - i * NC;
+      const int64_t ind = (int64_t)s_j[i] * a.stride + a.offset;
+      double *out;
+      int64_t e;
+      if (DH) {
+        out = a.hess_out;
+        e = 6 * ind + k;
+      } else if (DF && k == 0) {
+        out = a.f_out;
+        e = ind;
+      } else {
+        out = a.grad_out;
+        e = 3 * ind + (k - (DF ? 1 : 0));
+      }
+      const double vr = (double)s_res[i * 2 * NC + 2 * k], vi = (double)s_res[i * 2 * NC + 2 * k + 1];
+      if (a.real_io) {
+        if (a.accum) out[e] += vr;
+        else out[e] = vr;
+      } else {
+        double2 *o2 = (double2 *)out + e;
+        if (a.accum) {
+          double2 t = *o2;
+          t.x += vr;
+          t.y += vi;
+          *o2 = t;
+        } else {
+          *o2 = make_double2(vr, vi);
+        }
+      }
+    }
   }
 }
 
 // ---------------------------------------------------------------------------
-// spreading B^T, tiled (compile-time cutoff CUT <= 16)
+// spreading B^T, tiled, without atomics on the tile: every thread owns one
+// (a, b) column of the (8+2m)^3 region over one half of its z range and keeps
+// that piece of the region in registers.  The nodes of the sub-problem are
+// staged in batches (window values, node values, corners) by all threads;
+// then every thread adds the batch's nodes whose 13x13 (a, b) footprint
+// covers its column:
+//   acc[z] += f psi_x[a-o0] psi_y[b-o1] * psi_z[z-o2]
+// with psi_z stored zero-padded in region coordinates so that the z loop is
+// branch-free and uses vector loads.  FP32 sums are blocked and compensated:
+// each batch is summed in FP32 and folded into hi with an exact TwoSum (the
+// residual stays in acc), so rounding does not grow with the number of nodes
+// per tile (clustered nodes).  The region is committed with one global
+// atomic per non-zero grid point.
 // ---------------------------------------------------------------------------
+template <int CUT, int TT>
+struct ColGeom {
+  static constexpr int R = TT + CUT - 1;             // region edge
+  static constexpr int ZL = (R + 1) / 2;             // z values per thread
+  static constexpr int HZ = ((ZL + 3) / 4) * 4;      // padded half row
+  static constexpr int RP = 2 * HZ;                  // padded z row
+  static constexpr int XY = ((2 * CUT + 3) / 4) * 4; // px, py block
+  static constexpr int WREC = RP + XY;
+  static constexpr int THREADS = ((R * R * 2 + 31) / 32) * 32;
+};
+
+template <typename T>
+__device__ __forceinline__ void two_sum(T &hi, T &lo) {
+  T s = hi + lo;
+  T bv = s - hi;
+  T e = (hi - (s - bv)) + (lo - bv);
+  hi = s;
+  lo = e;
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void load_row(const T *p, T *v);
+template <int N>
+__device__ __forceinline__ void load_row(const float *p, float *v) {
+#pragma unroll
+  for (int q = 0; q < N / 4; q++) {
+    float4 t = ((const float4 *)p)[q];
+    v[4 * q] = t.x;
+    v[4 * q + 1] = t.y;
+    v[4 * q + 2] = t.z;
+    v[4 * q + 3] = t.w;
+  }
+}
+template <int N>
+__device__ __forceinline__ void load_row(const double *p, double *v) {
+#pragma unroll
+  for (int q = 0; q < N / 2; q++) {
+    double2 t = ((const double2 *)p)[q];
+    v[2 * q] = t.x;
+    v[2 * q + 1] = t.y;
+  }
+}
+
 template <typename T, int CUT, int MODE>
-__global__ void __launch_bounds__(256) k_spread_tile(ConvArgs a) {
+__global__ void __launch_bounds__(ColGeom<CUT, 8>::THREADS) k_spread_cols(ConvArgs a) {
   typedef typename Cplx<T>::type C;
+  typedef ColGeom<CUT, 8> G;
+  constexpr int R = G::R, ZL = G::ZL, HZ = G::HZ, RP = G::RP, WREC = G::WREC;
   constexpr bool DF = (MODE & 1) != 0, DG = (MODE & 2) != 0;
   constexpr int NDER = DG ? 1 : 0;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int NB = sizeof(T) == 4 ? 32 : 16;  // nodes per batch
+  constexpr int WSZ = (DG ? 2 : 1) * WREC;
+  // per node: [pz (RP)][px (CUT)][py (CUT)][pad] and, with DG, the same for the derivatives
+  __shared__ __align__(16) T s_w[NB][WSZ];
+  __shared__ T s_v[NB][8];  // f re/im, g0..g2 re/im (already scaled)
+  __shared__ T s_d[NB][4];
+  __shared__ int s_o[NB];
   const Binning &b = a.bin;
   const int sub = blockIdx.x;
   if (sub >= *b.nsub) return;
   const int tile = b.sub_tile[sub], first = b.sub_first[sub], cnt = b.sub_cnt[sub];
   int base[3];
   tile_base(b, tile, base);
-  const int R0 = b.T[0] + CUT - 1, R1 = b.T[1] + CUT - 1, R2 = b.T[2] + CUT - 1;
-  const int vol = R0 * R1 * R2;
-  T *sre = (T *)smem_raw;
-  T *sim = sre + vol;
-  T *wsall = sim + vol;
-  for (int i = threadIdx.x; i < vol; i += blockDim.x) {
-    sre[i] = (T)0;
-    sim[i] = (T)0;
-  }
-  __syncthreads();
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-  T *ws = wsall + warp * (6 * CUT);
-  const int row = lane >> 4, col = lane & 15;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int colid = tid >> 1, zh = tid & 1;
+  const bool active = colid < R * R;
+  const int ca = active ? colid / R : 0, cb = active ? colid % R : 0;
+  constexpr bool COMP = sizeof(T) == 4;
+  constexpr int ZC = COMP ? ZL : 1;
+  T acc_r[ZL], acc_i[ZL], hi_r[ZC], hi_i[ZC];
+#pragma unroll
+  for (int z = 0; z < ZL; z++) acc_r[z] = acc_i[z] = (T)0;
+#pragma unroll
+  for (int z = 0; z < ZC; z++) hi_r[z] = hi_i[z] = (T)0;
   const T scale = a.use_il ? (T)0.5 : (T)1;
-  for (int q = warp; q < cnt; q += nwarp) {
-    const int j = b.perm[first + q];
-    double dist[3];
-    int o[3];
-#pragma unroll
-    for (int t = 0; t < 3; t++) {
-      AxisPos p = axis_pos(a.x[3 * (int64_t)j + t], a.w.n[t], a.w.m, a.il);
-      dist[t] = p.dist;
-      o[t] = p.u - base[t];
-    }
-    warp_windows<T>(a.w, dist, NDER, ws, lane);
-    const int64_t ind = (int64_t)j * a.stride + a.offset;
-    T f_r = 0, f_i = 0;
-    T g_r[3] = {0, 0, 0}, g_i[3] = {0, 0, 0};
-    if (DF) {
-      if (a.real_io) f_r = (T)a.f_in[ind];
-      else {
-        f_r = (T)a.f_in[2 * ind];
-        f_i = (T)a.f_in[2 * ind + 1];
-      }
-      f_r *= scale;
-      f_i *= scale;
-    }
-    if (DG) {
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        if (a.real_io) g_r[c] = (T)a.grad_in[3 * ind + c];
+  for (int b0 = 0; b0 < cnt; b0 += NB) {
+    const int nb = min(NB, cnt - b0);
+    __syncthreads();
+    // --- stage node data and clear the padded z rows -------------------------
+    for (int i = tid; i < nb; i += nth) {
+      const int q = first + b0 + i;
+      T d[3];
+      int pk;
+      load_rec_raw(b.rec, q, d, &pk);
+      s_d[i][0] = d[0];
+      s_d[i][1] = d[1];
+      s_d[i][2] = d[2];
+      s_o[i] = pk;
+      const int64_t ind = (int64_t)b.perm[q] * a.stride + a.offset;
+      T v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (DF) {
+        if (a.real_io) v[0] = (T)a.f_in[ind];
         else {
-          g_r[c] = (T)a.grad_in[2 * (3 * ind + c)];
-          g_i[c] = (T)a.grad_in[2 * (3 * ind + c) + 1];
+          double2 f = ((const double2 *)a.f_in)[ind];
+          v[0] = (T)f.x;
+          v[1] = (T)f.y;
         }
-        g_r[c] *= scale;
-        g_i[c] *= scale;
       }
-    }
-    __syncwarp();
-    T px[CUT], dpx[CUT];
+      if (DG) {
 #pragma unroll
-    for (int l = 0; l < CUT; l++) {
-      px[l] = ws[l];
-      if (DG) dpx[l] = ws[3 * CUT + l];
-    }
-    if (col < CUT) {
-      const T pz = ws[2 * CUT + col];
-      const T dz = DG ? ws[3 * CUT + 2 * CUT + col] : (T)0;
-      for (int l1 = row; l1 < CUT; l1 += 2) {
-        const T py = ws[CUT + l1];
-        const T dy = DG ? ws[3 * CUT + CUT + l1] : (T)0;
-        // w(l0) = px[l0] * c1 + dpx[l0] * c2
-        T c1_r = 0, c1_i = 0, c2_r = 0, c2_i = 0;
-        if (DF) {
-          c1_r = py * pz * f_r;
-          c1_i = py * pz * f_i;
-        }
-        if (DG) {
-          c1_r += dy * pz * g_r[1] + py * dz * g_r[2];
-          c1_i += dy * pz * g_i[1] + py * dz * g_i[2];
-          c2_r = py * pz * g_r[0];
-          c2_i = py * pz * g_i[0];
-        }
-        const int rb = ((o[0]) * R1 + (o[1] + l1)) * R2 + (o[2] + col);
-#pragma unroll
-        for (int l0 = 0; l0 < CUT; l0++) {
-          T wr = px[l0] * c1_r, wi = px[l0] * c1_i;
-          if (DG) {
-            wr += dpx[l0] * c2_r;
-            wi += dpx[l0] * c2_i;
+        for (int c = 0; c < 3; c++) {
+          if (a.real_io) v[2 + 2 * c] = (T)a.grad_in[3 * ind + c];
+          else {
+            double2 g = ((const double2 *)a.grad_in)[3 * ind + c];
+            v[2 + 2 * c] = (T)g.x;
+            v[3 + 2 * c] = (T)g.y;
           }
-          atomicAdd(&sre[rb + l0 * R1 * R2], wr);
-          atomicAdd(&sim[rb + l0 * R1 * R2], wi);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 8; c++) s_v[i][c] = v[c] * scale;
+    }
+    for (int v = tid; v < nb * RP; v += nth) {
+      const int i = v / RP, z = v - i * RP;
+      s_w[i][z] = (T)0;
+      if (DG) s_w[i][WREC + z] = (T)0;
+    }
+    __syncthreads();
+    // --- window values: all threads over (node, axis, stencil point) ----------
+    for (int v = tid; v < nb * 3 * CUT; v += nth) {
+      const int i = v / (3 * CUT), e = v - i * 3 * CUT;
+      const int t = e / CUT, sidx = e - t * CUT;
+      T out[3];
+      window_point<T>(a.w, t, sidx, s_d[i][t], NDER, out);
+      int pos;
+      if (t < 2) {
+        pos = RP + t * CUT + sidx;
+      } else {
+        const int z = ((s_o[i] >> 16) & 0xff) + sidx;  // region z of this stencil point
+        pos = (z < ZL) ? z : HZ + (z - ZL);
+      }
+      s_w[i][pos] = out[0];
+      if (DG) s_w[i][WREC + pos] = out[1];
+    }
+    __syncthreads();
+    // --- accumulate the batch, then fold into hi -------------------------------
+    if (active) {
+      for (int i = 0; i < nb; i++) {
+        const int pk = s_o[i];
+        const int da = ca - (pk & 0xff), db = cb - ((pk >> 8) & 0xff);
+        if ((unsigned)da < (unsigned)CUT && (unsigned)db < (unsigned)CUT) {
+          const T *w = s_w[i];
+          const T pxy = w[RP + da] * w[RP + CUT + db];
+          T h1r = 0, h1i = 0, h2r = 0, h2i = 0;
+          if (DF) {
+            h1r = pxy * s_v[i][0];
+            h1i = pxy * s_v[i][1];
+          }
+          if (DG) {
+            const T *wd = w + WREC;
+            const T dxy = wd[RP + da] * w[RP + CUT + db], xdy = w[RP + da] * wd[RP + CUT + db];
+            h1r += dxy * s_v[i][2] + xdy * s_v[i][4];
+            h1i += dxy * s_v[i][3] + xdy * s_v[i][5];
+            h2r = pxy * s_v[i][6];
+            h2i = pxy * s_v[i][7];
+          }
+          T pz[HZ];
+          load_row<HZ>(w + zh * HZ, pz);
+#pragma unroll
+          for (int z = 0; z < ZL; z++) {
+            acc_r[z] += h1r * pz[z];
+            acc_i[z] += h1i * pz[z];
+          }
+          if (DG) {
+            T dz[HZ];
+            load_row<HZ>(w + WREC + zh * HZ, dz);
+#pragma unroll
+            for (int z = 0; z < ZL; z++) {
+              acc_r[z] += h2r * dz[z];
+              acc_i[z] += h2i * dz[z];
+            }
+          }
+        }
+      }
+      if (COMP) {
+#pragma unroll
+        for (int z = 0; z < ZC; z++) {
+          two_sum(hi_r[z], acc_r[z]);
+          two_sum(hi_i[z], acc_i[z]);
         }
       }
     }
-    __syncwarp();
   }
-  __syncthreads();
+  // --- commit the region ---------------------------------------------------------
+  if (!active) return;
   const int n0 = a.w.n[0], n1 = a.w.n[1], n2 = a.w.n[2];
-  C *grid = (C *)a.grid;
-  for (int i = threadIdx.x; i < vol; i += blockDim.x) {
+  const int g0 = (base[0] + ca) % n0, g1 = (base[1] + cb) % n1;
+  C *grid = (C *)a.grid + ((size_t)g0 * n1 + g1) * n2;
+  const int z0 = zh * ZL;
+#pragma unroll
+  for (int z = 0; z < ZL; z++) {
+    const int zz = z0 + z;
+    if (zz >= R) break;
     C v;
-    v.x = sre[i];
-    v.y = sim[i];
+    if (COMP) {
+      v.x = hi_r[z < ZC ? z : 0] + acc_r[z];
+      v.y = hi_i[z < ZC ? z : 0] + acc_i[z];
+    } else {
+      v.x = acc_r[z];
+      v.y = acc_i[z];
+    }
     if (v.x == (T)0 && v.y == (T)0) continue;
-    int c = i % R2, q = i / R2;
-    int bb = q % R1, aa = q / R1;
-    int g0 = (base[0] + aa) % n0, g1 = (base[1] + bb) % n1, g2 = (base[2] + c) % n2;
-    atomic_add_grid(&grid[((size_t)g0 * n1 + g1) * n2 + g2], v);
+    atomic_add_grid(&grid[(base[2] + zz) % n2], v);
   }
 }
 
@@ -496,20 +808,10 @@ __global__ void k_interp_generic(ConvArgs a) {
     dist[t] = p.dist;
     u[t] = p.u;
   }
-  // single-thread window evaluation: reuse warp_windows with a 1-lane stride
   for (int e = 0; e < 3 * cut; e++) {
     int t = e / cut, s = e - t * cut;
     T out[3] = {(T)0, (T)0, (T)0};
-    if (a.w.intpol_order >= 0) {
-      double dK = dist[t] * (double)a.w.intpol_K;
-      long long k = (long long)floor(dK);
-      T dk = (T)(dK - (double)k);
-      size_t bse = ((size_t)k * cut + s) * (size_t)(a.w.intpol_order + 1);
-      for (int d = 0; d <= NDER; d++) out[d] = intpol<T>(a.w.intpol_order, (const T *)a.w.tab[d][t] + bse, dk);
-    } else {
-      window_eval<T>(a.w.kind, a.w.m, (T)a.w.n[t], (T)a.w.b[t], (T)dist[t] + (T)(a.w.m - s), (T)s - (T)dist[t], NDER,
-                     out);
-    }
+    window_point<T>(a.w, t, s, (T)dist[t], NDER, out);
     ws[e] = out[0];
     ws[3 * cut + e] = out[1];
     ws[6 * cut + e] = out[2];
@@ -598,16 +900,7 @@ __global__ void k_spread_generic(ConvArgs a) {
   for (int e = 0; e < 3 * cut; e++) {
     int t = e / cut, s = e - t * cut;
     T out[3] = {(T)0, (T)0, (T)0};
-    if (a.w.intpol_order >= 0) {
-      double dK = dist[t] * (double)a.w.intpol_K;
-      long long k = (long long)floor(dK);
-      T dk = (T)(dK - (double)k);
-      size_t bse = ((size_t)k * cut + s) * (size_t)(a.w.intpol_order + 1);
-      for (int d = 0; d <= NDER; d++) out[d] = intpol<T>(a.w.intpol_order, (const T *)a.w.tab[d][t] + bse, dk);
-    } else {
-      window_eval<T>(a.w.kind, a.w.m, (T)a.w.n[t], (T)a.w.b[t], (T)dist[t] + (T)(a.w.m - s), (T)s - (T)dist[t], NDER,
-                     out);
-    }
+    window_point<T>(a.w, t, s, (T)dist[t], NDER, out);
     ws[e] = out[0];
     ws[3 * cut + e] = out[1];
   }
@@ -665,37 +958,19 @@ __global__ void k_spread_generic(ConvArgs a) {
 static const int kThreads = 256;
 
 void choose_tiles(int cut, bool fp32, const int *n, int *T) {
-  // largest cubic tile whose halo-padded region fits the shared-memory budget
-  const size_t budget = fp32 ? 112 * 1024 : 136 * 1024;
-  const size_t elem = fp32 ? 8 : 16;
-  int t = 16;
-  while (t > 1) {
-    size_t r = (size_t)(t + cut - 1);
-    if (r * r * r * elem <= budget) break;
-    t >>= 1;
-  }
-  if (fp32 && t > 8) t = 8;
-  for (int d = 0; d < 3; d++) {
-    int td = t;
-    while (td > 1 && td > n[d]) td >>= 1;
-    T[d] = td;
-  }
-}
-
-size_t conv_smem_bytes(const int *T, int cut, bool fp32, bool spread) {
-  size_t vol = (size_t)(T[0] + cut - 1) * (T[1] + cut - 1) * (T[2] + cut - 1);
-  size_t elem = fp32 ? 4 : 8;
-  size_t region = vol * 2 * elem;
-  size_t scratch = (size_t)(kThreads / 32) * (spread ? 6 : 9) * cut * elem;
-  return region + scratch;
+  // 8x8x8 cells per tile: the interpolation stages the (8+2m)^3 region in
+  // shared memory (FP64, m=7: 170 KB), the spreading keeps it in registers
+  (void)cut;
+  (void)fp32;
+  for (int d = 0; d < 3; d++) T[d] = n[d] >= 8 ? 8 : n[d];
 }
 
 template <typename T, int CUT, int MODE>
 static void run_interp_tile(const ConvArgs &a, cudaStream_t s) {
-  size_t sm = conv_smem_bytes(a.bin.T, CUT, sizeof(T) == 4, false);
+  const size_t sm = InterpGeom<T, CUT, MODE>::SMEM;
   static bool attr_done = false;
   if (!attr_done) {
-    cudaFuncSetAttribute(k_interp_tile<T, CUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_interp_tile<T, CUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     attr_done = true;
   }
   k_interp_tile<T, CUT, MODE><<<a.bin.max_subs, kThreads, sm, s>>>(a);
@@ -703,13 +978,7 @@ static void run_interp_tile(const ConvArgs &a, cudaStream_t s) {
 
 template <typename T, int CUT, int MODE>
 static void run_spread_tile(const ConvArgs &a, cudaStream_t s) {
-  size_t sm = conv_smem_bytes(a.bin.T, CUT, sizeof(T) == 4, true);
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaFuncSetAttribute(k_spread_tile<T, CUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    attr_done = true;
-  }
-  k_spread_tile<T, CUT, MODE><<<a.bin.max_subs, kThreads, sm, s>>>(a);
+  k_spread_cols<T, CUT, MODE><<<a.bin.max_subs, ColGeom<CUT, 8>::THREADS, 0, s>>>(a);
 }
 
 template <typename T, int MODE>
@@ -739,15 +1008,14 @@ static bool spread_by_cut(const ConvArgs &a, cudaStream_t s) {
 }
 
 static bool tiles_usable(const ConvArgs &a) {
-  size_t sm = conv_smem_bytes(a.bin.T, a.w.cut, false, false);
-  return a.w.cut <= 15 && sm <= 200 * 1024;
+  return a.w.cut <= 15 && a.bin.T[0] == 8 && a.bin.T[1] == 8 && a.bin.T[2] == 8;
 }
 
 template <typename T>
 static void interp_t(const ConvArgs &a, int mode, cudaStream_t s) {
   if (a.M == 0) return;
   bool done = false;
-  if (tiles_usable(a) || sizeof(T) == 4) {
+  if (tiles_usable(a)) {
     switch (mode) {
       case 1: done = interp_by_cut<T, 1>(a, s); break;
       case 2: done = interp_by_cut<T, 2>(a, s); break;
@@ -771,7 +1039,7 @@ template <typename T>
 static void spread_t(const ConvArgs &a, int mode, cudaStream_t s) {
   if (a.M == 0) return;
   bool done = false;
-  if (tiles_usable(a) || sizeof(T) == 4) {
+  if (tiles_usable(a)) {
     switch (mode) {
       case 1: done = spread_by_cut<T, 1>(a, s); break;
       case 2: done = spread_by_cut<T, 2>(a, s); break;

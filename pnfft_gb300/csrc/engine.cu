@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <stdio.h>
+#include <math.h>
 #include <string.h>
 
 #include <algorithm>
@@ -194,6 +195,11 @@ static void free_binning(Binning &b) {
     if (*a) cudaFree(*a);
     *a = nullptr;
   }
+  if (b.rec) cudaFree(b.rec);
+  if (b.rec_tmp) cudaFree(b.rec_tmp);
+  if (b.bsum) cudaFree(b.bsum);
+  b.rec = b.rec_tmp = nullptr;
+  b.bsum = nullptr;
 }
 
 static int ensure_binning(pnfft_plan p, int64_t M) {
@@ -202,7 +208,7 @@ static int ensure_binning(pnfft_plan p, int64_t M) {
   int T[3];
   choose_tiles(p->cutoff, fp32(p), n, T);
   bool same_tiles = T[0] == d->bin_T[0] && T[1] == d->bin_T[1] && T[2] == d->bin_T[2];
-  if (same_tiles && d->bin_cap_M >= M && d->bin[0].key) return 0;
+  if (same_tiles && d->bin_cap_M >= M && d->bin[0].key && d->bin_prec == p->precision) return 0;
   int64_t cap = std::max<int64_t>(M, std::max<int64_t>(d->bin_cap_M, 1));
   for (int ps = 0; ps < 2; ps++) {
     Binning &b = d->bin[ps];
@@ -225,9 +231,13 @@ static int ensure_binning(pnfft_plan p, int64_t M) {
     PG_CUDA(cudaMalloc(&b.sub_first, sizeof(int) * b.max_subs));
     PG_CUDA(cudaMalloc(&b.sub_cnt, sizeof(int) * b.max_subs));
     PG_CUDA(cudaMalloc(&b.nsub, sizeof(int)));
+    PG_CUDA(cudaMalloc(&b.rec, (fp32(p) ? sizeof(float4) : sizeof(double4)) * cap));
+    PG_CUDA(cudaMalloc(&b.rec_tmp, (fp32(p) ? sizeof(float4) : sizeof(double4)) * cap));
+    PG_CUDA(cudaMalloc(&b.bsum, sizeof(int) * 2 * ((b.ntiles + 2047) / 2048 + 1)));
     d->bin_valid[ps] = false;
   }
   d->bin_cap_M = cap;
+  d->bin_prec = p->precision;
   for (int t = 0; t < 3; t++) d->bin_T[t] = T[t];
   return 0;
 }
@@ -319,6 +329,17 @@ static WindowArgs window_args(pnfft_plan p) {
   for (int t = 0; t < 3; t++) {
     w.n[t] = (int)p->n[t];
     w.b[t] = p->b[t];
+    const double b = p->b[t];
+    WinF &c = w.wf[t];
+    c.n = (float)p->n[t];
+    c.b = (float)b;
+    c.b_lo = (float)(b - (double)c.b);
+    const double ib = (b != 0.0) ? 1.0 / b : 0.0, pb = (b != 0.0) ? kPi / b : 0.0;
+    c.ib = (float)ib;
+    c.ib_lo = (float)(ib - (double)c.ib);
+    c.pb = (float)pb;
+    c.pb_lo = (float)(pb - (double)c.pb);
+    c.gnorm = (b > 0.0) ? (float)(1.0 / sqrt(kPi * b)) : 0.f;
   }
   w.intpol_order = p->intpol_order;
   w.intpol_K = (int)p->intpol_K;
@@ -357,7 +378,7 @@ static int do_binning(pnfft_plan p, pnfft_nodes nd, ConvArgs &a, int il, int adj
   bool reuse = nd->fixed && d->bin_valid[il] && d->bin_uid[il] == nd->uid && d->bin_ver[il] == nd->version;
   if (!reuse) {
     StageScope sc(d, PNFFT_TIMER_SORT_NODES, adj);
-    bin_nodes(a, d->stream);
+    bin_nodes(a, fp32(p), d->stream);
     d->bin_valid[il] = true;
     d->bin_uid[il] = nd->uid;
     d->bin_ver[il] = nd->version;
@@ -523,6 +544,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
         const int il = il_plan ? pass : 0;
         ca.use_il = il_plan ? 1 : 0;
         ca.il = il;
+        ca.accum = (pass > 0 || (cflags & PNFFT_COMPUTE_ACCUMULATED)) ? 1 : 0;
         da.interlaced = il;
         if (nd && !(cflags & PNFFT_OMIT_CONV)) do_binning(p, nd, ca, il, 0);
         auto one = [&](int ikmode, int ikdim, double *out, int64_t off, int64_t stride, int mode) -> int {
@@ -794,7 +816,7 @@ int engine_node_index(pnfft_plan p, int64_t M, const double *x, int interlaced, 
   PG_CUDA(cudaMallocAsync(&du, sizeof(long long) * 3 * M, s));
   PG_CUDA(cudaMemcpyAsync(dx, x, sizeof(double) * 3 * M, cudaMemcpyHostToDevice, s));
   int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
-  launch_node_index(dx, M, n, p->m, interlaced, du, s);
+  launch_node_index(dx, M, n, p->m, interlaced, fp32(p), du, s);
   PG_CUDA(cudaMemcpyAsync(u, du, sizeof(long long) * 3 * M, cudaMemcpyDeviceToHost, s));
   cudaFreeAsync(dx, s);
   cudaFreeAsync(du, s);

@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "pg_math.cuh"
+
 namespace pg {
 
 // Window description shared by the convolution kernels.
@@ -13,6 +15,7 @@ struct WindowArgs {
   int m, cut;         // cutoff = 2m+1
   int n[3];           // oversampled grid
   double b[3];        // shape parameters
+  WinF wf[3];         // FP32 constants of each axis for the FP32-mixed kernels
   int intpol_order;   // -1: evaluate directly; 0..3: tabulated (PNFFT_PRE_*_PSI)
   int intpol_K;       // samples per grid cell of the tables
   const void *tab[3][3];  // [derivative][axis], element type = compute precision
@@ -35,6 +38,10 @@ struct Binning {
   int *sub_first;  // [max_subs]
   int *sub_cnt;    // [max_subs]
   int *nsub;       // [1]
+  void *rec;       // [M] node records in tile order: float4 (FP32-mixed) or double4
+                   // {dist0, dist1, dist2, local stencil corner o0 | o1<<8 | o2<<16}
+  void *rec_tmp;   // [M] the same records in node order (before the scatter)
+  int *bsum;       // [2 * ceil(ntiles / 2048)] scan block sums
 };
 
 // One convolution (B or B^T) launch.
@@ -44,6 +51,7 @@ struct ConvArgs {
   int real_only;    // read only the real parts of the grid (c2r and the
                     // c2c + PNFFT_PRE_QUAD_PSI behaviour of the reference)
   int real_io;      // node arrays are real (c2r) instead of complex
+  int accum;        // add into the node outputs (else store): ACCUMULATED, 2nd interlaced pass
   int64_t M;
   const double *x;  // [M][3]
   void *grid;       // n0*n1*n2 complex in compute precision, natural order
@@ -56,11 +64,10 @@ struct ConvArgs {
 
 // Launchers (conv.cu).  `fp32` selects the FP32-mixed kernels.  `mode` is a
 // bit set of 1 = f, 2 = grad, 4 = hessian (interp) / 1 = f, 2 = grad (spread).
-void bin_nodes(const ConvArgs &a, cudaStream_t s);
+void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s);
 void launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
 void launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
 void choose_tiles(int cut, bool fp32, const int *n, int *T);
-size_t conv_smem_bytes(const int *T, int cut, bool fp32, bool spread);
 
 // Deconvolution (deconv.cu).
 struct DeconvArgs {
@@ -79,7 +86,8 @@ void launch_deconv_pad(const DeconvArgs &a, bool fp32, cudaStream_t s);
 void launch_deconv_crop_acc(const DeconvArgs &a, bool fp32, cudaStream_t s);
 
 // Verification helpers and the direct NDFT (sort.cu, ndft.cu).
-void launch_node_index(const double *x, int64_t M, const int *n, int m, int il, long long *u, cudaStream_t s);
+void launch_node_index(const double *x, int64_t M, const int *n, int m, int il, bool integer_path, long long *u,
+                       cudaStream_t s);
 int radix_sort_nodes(const double *x, int64_t M, const int *n, int m, long long *pairs_dev, cudaStream_t s);
 
 struct NdftArgs {

@@ -207,6 +207,297 @@ PG_HD void window_eval(int kind, int m, T n, T b, T y, T s_minus_dist, int nder,
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 window evaluation with a compensated argument.
+//
+// In FP32 the window argument y = (m - s) + dist carries a rounding error of
+// ~ulp(m) (5e-7 at m = 6), and the windows grow like exp(b sqrt(m^2 - y^2))
+// (b m ~ 28 for Kaiser-Bessel at sigma = 2), which turns that error into a
+// ~2e-6 relative error of every weight.  Here y = k + d (k integer, 0 <= d < 1)
+// is kept as an exact two-float, and m^2 - y^2 = (m^2 - k^2) - d (2k + d),
+// sqrt, b*r, y^2/b and pi*y/b are carried as float pairs (TwoSum / TwoProd
+// with fmaf), so the exponentials see an argument accurate to ~1e-7 absolute.
+// ---------------------------------------------------------------------------
+struct WinF {
+  float n;             // grid size
+  float b, b_lo;       // shape parameter as a float pair
+  float ib, ib_lo;     // 1/b
+  float pb, pb_lo;     // pi/b
+  float gnorm;         // 1/sqrt(pi b) (Gaussian)
+};
+
+PG_HD void two_sum_f(float a, float b, float &s, float &e) {
+  s = a + b;
+  float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+PG_HD void two_prod_f(float a, float b, float &p, float &e) {
+  p = a * b;
+  e = fmaf(a, b, -p);
+}
+
+// M_p(j + phi) for integer j and phi in [0,1), Cox-de Boor on the pieces with
+// the integer and fractional parts kept apart:
+//   M_k(phi+i) = (i M_{k-1}(phi+i) + (k-i) M_{k-1}(phi+i-1) + phi (M_{k-1}(phi+i) - M_{k-1}(phi+i-1))) / (k-1)
+PG_HD float bspline_jphi(int p, int j, float phi) {
+  if (p < 1 || j < 0 || j >= p || (j == 0 && phi == 0.f)) return 0.f;
+  float v[40];
+  v[0] = 1.f;
+  for (int k = 2; k <= p; k++) {
+    float prev = 0.f;
+    const float inv = 1.f / (float)(k - 1);
+    for (int i = 0; i < k; i++) {
+      float cur = (i <= k - 2) ? v[i] : 0.f;
+      v[i] = (((float)i * cur + (float)(k - i) * prev) + phi * (cur - prev)) * inv;
+      prev = cur;
+    }
+  }
+  return v[j];
+}
+
+// I0 and I1 in FP32: power series below x = 12; above it the asymptotic
+// expansion I_nu(x) ~ e^x / sqrt(2 pi x) sum_k (-1)^k a_k(nu) / x^k with
+// a_k(nu) = prod_{j=1..k} (4 nu^2 - (2j-1)^2) / (k! 8^k) (Abramowitz & Stegun
+// 9.7.1), whose terms stay below 1e-8 after nine of them at x >= 12; the
+// series would accumulate ~1e-6 relative rounding over its ~20 growing terms.
+PG_HD void bessel_i01_f(float x, float &i0, float &i1) {
+  if (x < 12.f) {
+    i0 = bessel_i0<float>(x);
+    i1 = bessel_i1<float>(x);
+    return;
+  }
+  const float e = expf(x) / sqrtf(2.f * 3.14159265358979f * x);
+  const float ix = 1.f / (8.f * x);
+  float t0 = 1.f, t1 = 1.f, s0 = 1.f, s1 = 1.f;
+  for (int k = 1; k <= 9; k++) {
+    const float q = (float)((2 * k - 1) * (2 * k - 1));
+    t0 *= q * ix / (float)k;
+    t1 *= (q - 4.f) * ix / (float)k;
+    s0 += t0;
+    s1 += t1;
+  }
+  i0 = e * s0;
+  i1 = e * s1;
+}
+
+// Taylor coefficients about z = 0 (z = b^2 (m^2 - y^2)) of the two radial
+// windows, used where the closed-form derivatives cancel (|z| < 9):
+//   Kaiser-Bessel  psi = (b/pi) S(z),  S(z) = sinh(sqrt z)/sqrt z = sum z^k / (2k+1)!
+//   Bessel-I0      psi = T(z) / 2,     T(z) = I0(sqrt z)        = sum z^k / (4^k k!^2)
+// Horner evaluation of f, f' and f'' with ten terms (|z|^10 / 21! < 1e-10).
+PG_HD void radial_series(bool kb, float z, float &f0, float &f1, float &f2) {
+  constexpr int K = 11;
+  float c[K];
+  c[0] = 1.f;
+#pragma unroll
+  for (int k = 1; k < K; k++)
+    c[k] = kb ? c[k - 1] / (float)((2 * k) * (2 * k + 1)) : c[k - 1] / (float)(4 * k * k);
+  f0 = c[K - 1];
+  f1 = (float)(K - 1) * c[K - 1];
+  f2 = (float)((K - 1) * (K - 2)) * c[K - 1];
+#pragma unroll
+  for (int k = K - 2; k >= 0; k--) {
+    f0 = fmaf(f0, z, c[k]);
+    if (k >= 1) f1 = fmaf(f1, z, (float)k * c[k]);
+    if (k >= 2) f2 = fmaf(f2, z, (float)(k * (k - 1)) * c[k]);
+  }
+}
+
+// h(a) = cot a - 1/a and h'(a) = 1/a^2 - 1 - cot^2 a for the sinc-power window.
+// Below |a| = 1, where the closed forms cancel, by the series
+//   cot a - 1/a = -sum_{j>=1} 2^(2j) |B_2j| a^(2j-1) / (2j)!
+// (B_2j the Bernoulli numbers; ten terms, the last below 3e-10 at |a| = 1).
+PG_HD void sinc_h(float a, float &h, float &hp) {
+  if (fabsf(a) < 1.f) {
+    const float c[10] = {1.f / 3.f,
+                         1.f / 45.f,
+                         2.f / 945.f,
+                         1.f / 4725.f,
+                         2.f / 93555.f,
+                         1382.f / 638512875.f,
+                         4.f / 18243225.f,
+                         3617.f / 162820783125.f,
+                         87734.f / 38979295480125.f,
+                         349222.f / 1531329465290625.f};
+    const float a2 = a * a;
+    float s = c[9], sp = 19.f * c[9];
+#pragma unroll
+    for (int j = 8; j >= 0; j--) {
+      s = fmaf(s, a2, c[j]);
+      sp = fmaf(sp, a2, (float)(2 * j + 1) * c[j]);
+    }
+    h = -a * s;
+    hp = -sp;
+  } else {
+    const float ct = 1.f / tanf(a);
+    h = ct - 1.f / a;
+    hp = 1.f / (a * a) - 1.f - ct * ct;
+  }
+}
+
+// window values at y = k + d, derivative order up to nder (out[0..2])
+PG_HD void window_eval_f(int kind, int m, const WinF &c, int k, float d, int nder, float *out) {
+  const float pi = 3.14159265358979f;
+  const float mm = (float)m, n = c.n;
+  float yh, yl;
+  two_sum_f((float)k, d, yh, yl);
+  const float y = yh;  // for the multiplicative factors
+  switch (kind) {
+    case WIN_GAUSSIAN: {
+      // q = y^2 = k^2 + d (2k + d), z = q / b
+      float s2, se, pr, pe, qh, ql, zh, zl;
+      two_sum_f((float)(2 * k), d, s2, se);
+      two_prod_f(d, s2, pr, pe);
+      pe += d * se;
+      two_sum_f((float)(k * k), pr, qh, ql);
+      ql += pe;
+      two_prod_f(qh, c.ib, zh, zl);
+      zl += qh * c.ib_lo + ql * c.ib;
+      const float psi = expf(-zh) * (1.f - zl) * c.gnorm;
+      out[0] = psi;
+      if (nder >= 1) out[1] = -2.f * n * c.ib * y * psi;
+      if (nder >= 2) out[2] = 2.f * n * n * c.ib * (2.f * c.ib * (qh + ql) - 1.f) * psi;
+      break;
+    }
+    case WIN_BSPLINE: {
+      // psi = M_2m(s - d), s = m - k
+      const int s = m - k;
+      int j;
+      float phi;
+      if (d > 0.f) {
+        j = s - 1;
+        phi = 1.f - d;
+      } else {
+        j = s;
+        phi = 0.f;
+      }
+      out[0] = bspline_jphi(2 * m, j, phi);
+      if (nder >= 1) out[1] = -n * (bspline_jphi(2 * m - 1, j, phi) - bspline_jphi(2 * m - 1, j - 1, phi));
+      if (nder >= 2)
+        out[2] = n * n *
+                 (bspline_jphi(2 * m - 2, j, phi) - 2.f * bspline_jphi(2 * m - 2, j - 1, phi) +
+                  bspline_jphi(2 * m - 2, j - 2, phi));
+      break;
+    }
+    case WIN_SINC_POWER: {
+      // a = pi y / b as a pair.  The 2m-th power multiplies the relative
+      // error of sinc(a) by 2m, so sinc is taken in FP64 (this window only)
+      // and its rounding to float is carried as a first-order correction.
+      float ah, al;
+      two_prod_f(c.pb, yh, ah, al);
+      al += c.pb * yl + c.pb_lo * yh;
+      const double ad = (double)ah + (double)al;
+      const double scd = sinc<double>(ad);
+      const float sc = (float)scd;
+      const float corr = (scd != 0.0) ? (float)((scd - (double)sc) / scd) : 0.f;
+      const float psi = powf(sc, 2.f * mm) * c.ib * (1.f + 2.f * mm * corr + c.ib_lo / c.ib);
+      out[0] = psi;
+      if (nder >= 1) {
+        // d/dx = 2m (pi n / b) h(a) psi;  d2/dx2 = 2m (pi n / b)^2 (h'(a) + 2m h(a)^2) psi
+        float h, hp;
+        sinc_h(ah, h, hp);
+        const float q = pi * n * c.ib;
+        out[1] = 2.f * mm * q * h * psi;
+        if (nder >= 2) out[2] = 2.f * mm * q * q * (hp + 2.f * mm * h * h) * psi;
+      }
+      break;
+    }
+    default: {  // Kaiser-Bessel and Bessel-I0: D = m^2 - y^2
+      float s2, se, pr, pe, Dh, Dl;
+      two_sum_f((float)(2 * k), d, s2, se);
+      two_prod_f(d, s2, pr, pe);
+      pe += d * se;
+      two_sum_f((float)(m * m - k * k), -pr, Dh, Dl);
+      Dl -= pe;
+      const float D = Dh + Dl;
+      const bool kb = (kind != WIN_BESSEL_I0);
+      const float b2 = c.b * c.b, z = b2 * D;
+      if (D == 0.f) {
+        // the values the reference assigns at |y| = m (both signs of y)
+        if (kb) {
+          out[0] = c.b / pi;
+          if (nder >= 1) out[1] = -n * mm * c.b * c.b * c.b / (3.f * pi);
+          if (nder >= 2) {
+            const float bn = c.b * n, bm = c.b * mm;
+            out[2] = c.b * bn * bn / (15.f * pi) * (bm * bm - 5.f);
+          }
+        } else {
+          out[0] = 0.5f;
+          if (nder >= 1) {
+            const float h = 0.5f * c.b * n;
+            out[1] = -h * h * y / n;
+          }
+          if (nder >= 2) {
+            const float t1 = c.b * c.b * mm * n, t2 = c.b * n;
+            out[2] = t1 * t1 / 16.f - t2 * t2 / 4.f;
+          }
+        }
+      } else if (!kb && D < 0.f) {
+        out[0] = 0.f;
+        if (nder >= 1) out[1] = 0.f;
+        if (nder >= 2) out[2] = 0.f;
+      } else if (fabsf(z) < 9.f) {
+        // psi = A f(z), dpsi/dx = -2 A n b^2 y f'(z), d2psi/dx2 = A n^2 (4 b^4 y^2 f'' - 2 b^2 f')
+        float f0, f1, f2;
+        radial_series(kb, z, f0, f1, f2);
+        const float A = kb ? c.b / pi : 0.5f;
+        out[0] = A * f0;
+        if (nder >= 1) out[1] = -2.f * A * n * b2 * y * f1;
+        if (nder >= 2) out[2] = A * n * n * b2 * (4.f * b2 * y * y * f2 - 2.f * f1);
+      } else if (D > 0.f) {
+        const float rh = sqrtf(D);
+        const float rl = (fmaf(-rh, rh, Dh) + Dl) / (2.f * rh);
+        float xh, xl;
+        two_prod_f(c.b, rh, xh, xl);
+        xl += c.b * rl + c.b_lo * rh;
+        if (kb) {
+          // xh >= 3 here
+          const float E = expf(xh) * (1.f + xl), Ei = 1.f / E;
+          const float sh = 0.5f * (E - Ei), ch = 0.5f * (E + Ei);
+          const float psi = sh / (pi * rh) * (1.f - rl / rh);
+          out[0] = psi;
+          float dpsi = 0.f;
+          if (nder >= 1) {
+            dpsi = n * y / D * (psi - c.b * ch / pi);
+            out[1] = dpsi;
+          }
+          if (nder >= 2) {
+            const float by = c.b * y;
+            out[2] = 3.f * n * y * dpsi / D + n * n * psi / D * (1.f + by * by) - c.b * n * n / (pi * D) * ch;
+          }
+        } else {
+          float i0h, i1h;
+          bessel_i01_f(xh, i0h, i1h);
+          out[0] = 0.5f * (i0h + i1h * xl);
+          const float r = rh + rl;
+          const float i1 = i1h + (i0h - i1h / xh) * xl;
+          if (nder >= 1) out[1] = -0.5f * c.b * n * y * i1 / r;
+          if (nder >= 2) {
+            const float yy = y * y;
+            out[2] = 0.5f * c.b * n * n / D * (c.b * yy * (i0h + i1h * xl) - i1 / r * (yy + mm * mm));
+          }
+        }
+      } else {  // Kaiser-Bessel continued as sin beyond |y| = m
+        const float r = sqrtf(-D), br = c.b * r;
+        float sn, cs;
+        sincosf(br, &sn, &cs);
+        const float psi = sn / (pi * r);
+        out[0] = psi;
+        float dpsi = 0.f;
+        if (nder >= 1) {
+          dpsi = n * y / D * (psi - c.b * cs / pi);
+          out[1] = dpsi;
+        }
+        if (nder >= 2) {
+          const float by = c.b * y;
+          out[2] = 3.f * n * y * dpsi / D + n * n * psi / D * (1.f + by * by) - c.b * n * n / (pi * D) * cs;
+        }
+      }
+      break;
+    }
+  }
+}
+
 // One-dimensional window at position x (units of [0,1)), as PNX(psi/dpsi/ddpsi)
 // of ndft-parallel.c:2288-2334.
 template <typename T>

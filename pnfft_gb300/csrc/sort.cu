@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "pg_index.cuh"
 #include "pg_kernels.h"
 
 namespace pg {
@@ -29,9 +30,25 @@ __global__ void k_node_index(const double *__restrict__ x, int64_t M, int n0, in
   }
 }
 
-void launch_node_index(const double *x, int64_t M, const int *n, int m, int il, long long *u, cudaStream_t s) {
+// the integer-only evaluation used by the FP32-mixed binning
+__global__ void k_node_index_exact(const double *__restrict__ x, int64_t M, int n0, int n1, int n2, int m,
+                                   long long *__restrict__ u) {
+  int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= M) return;
+  const int n[3] = {n0, n1, n2};
+  for (int t = 0; t < 3; t++) {
+    long long fnx;
+    float fr;
+    nx_exact(x[3 * j + t], n[t], &fnx, &fr);
+    u[3 * j + t] = fnx - m;
+  }
+}
+
+void launch_node_index(const double *x, int64_t M, const int *n, int m, int il, bool integer_path, long long *u,
+                       cudaStream_t s) {
   if (M <= 0) return;
-  k_node_index<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(x, M, n[0], n[1], n[2], m, il, u);
+  if (integer_path && !il) k_node_index_exact<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(x, M, n[0], n[1], n[2], m, u);
+  else k_node_index<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(x, M, n[0], n[1], n[2], m, il, u);
 }
 
 // key of ndft-parallel.c:2131-2142; n*x - m evaluated without FMA

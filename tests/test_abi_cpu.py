@@ -100,6 +100,17 @@ def test_invalid_plans_return_null(lib):
     np3 = (ctypes.c_int * 3)(1, 1, 1)
     assert L.pnfft_create_procmesh(3, lib.MPI_COMM_WORLD, np3, ctypes.byref(out)) == 0
     assert out.value == lib.MPI_COMM_WORLD
+    # FP32-mixed refuses radial windows that overflow FP32 (b*m >= 80)
+    n = (ctypes.c_ssize_t * 3)(64, 64, 64)
+    N = (ctypes.c_ssize_t * 3)(32, 32, 32)
+    assert not L.pnfft_init_guru(3, N, n, xm, 17, lib.GB300_FP32, 0, lib.MPI_COMM_WORLD)
+    assert "overflows FP32" in lib.last_error()
+    p = L.pnfft_init_guru(3, N, n, xm, 17, 0, 0, lib.MPI_COMM_WORLD)
+    assert p and L.pnfft_gb300_set_precision(p, 1) == -1
+    L.pnfft_finalize(p, 0)
+    p = L.pnfft_init_guru(3, N, n, xm, 16, lib.GB300_FP32, 0, lib.MPI_COMM_WORLD)
+    assert p and L.pnfft_gb300_get_precision(p) == 1
+    L.pnfft_finalize(p, 0)
 
 
 def test_rand_generators_match_oracle(lib, oracle):

@@ -161,9 +161,20 @@ def test_node_index_and_sort_bitexact(gpu, oracle):
         x[t * edge.size:(t + 1) * edge.size, t] = edge
     x[5000:6000] = x[17]
     p = gpu.Plan(N, n, m=m)
+    p32 = gpu.Plan(N, n, m=m, precision="fp32")  # integer-only index path
     o = oracle.OraclePlan(N, n, m=m)
     for il in (0, 1):
-        np.testing.assert_array_equal(p.node_index(x, il), o.node_index(x, il)[0])
+        want = o.node_index(x, il)[0]
+        np.testing.assert_array_equal(p.node_index(x, il), want)
+        np.testing.assert_array_equal(p32.node_index(x, il), want)
+    # wider coverage of the integer path: many magnitudes, odd grid sizes
+    rng2 = np.random.default_rng(10)
+    xs = np.concatenate([rng2.uniform(-0.5, 0.5, (4000, 3)),
+                         (rng2.uniform(-1, 1, (2000, 3)) * 10.0 ** rng2.integers(-12, 0, (2000, 3))) % 1 - 0.5,
+                         rng2.uniform(-1, 1, (2000, 3)) * 10.0 ** rng2.integers(-300, 0, (2000, 3))])
+    for nn in [(17, 1023, 1000), (96, 129, 2048)]:
+        a = gpu.Plan((8, 8, 8), nn, m=3, precision="fp32")
+        np.testing.assert_array_equal(a.node_index(xs), oracle.OraclePlan((8, 8, 8), nn, m=3).node_index(xs)[0])
     np.testing.assert_array_equal(p.sort_nodes(x), o.sort_nodes(x))
 
 
@@ -186,6 +197,40 @@ def test_fp32_mixed_vs_ndft(gpu, oracle):
     a = p.adj(x, fv)
     ad = o.adj(x, fv, None, 1 | gpu.COMPUTE_DIRECT)
     assert rel(a, ad) < 2e-6
+
+
+def test_fp32_tiny_and_edge_coordinates(gpu, oracle):
+    # coordinates whose product n*x lies below 2^-11 (the whole product is
+    # fraction), signed zeros, subnormals and the ends of [-0.5, 0.5)
+    N = (16, 16, 16)
+    rng = np.random.default_rng(33)
+    special = np.array([0.0, -0.0, 1.03e-5, -1.03e-5, 3e-9, -3e-9, 1e-300, -1e-300, 5e-324, -5e-324,
+                        -0.5, 0.5 - 2.0 ** -53, 2.0 ** -16, -2.0 ** -16])
+    x = rng.uniform(-0.5, 0.5, (3 * special.size, 3))
+    for t in range(3):
+        x[t * special.size:(t + 1) * special.size, t] = special
+    fh = rng.standard_normal(4096) + 1j * rng.standard_normal(4096)
+    f = rng.standard_normal(x.shape[0]) + 1j * rng.standard_normal(x.shape[0])
+    p = gpu.Plan(N, m=6, precision="fp32")
+    o = oracle.OraclePlan(N, m=6)
+    got, want = p.trafo(x, fh)[0], o.trafo(x, fh)[0]
+    assert np.abs(got - want).max() <= 2e-6 * np.abs(want).max()
+    assert rel(p.adj(x, f), o.adj(x, f)) < 2e-6
+
+
+@pytest.mark.parametrize("win", list(WINDOWS))
+def test_fp32_mixed_all_windows_vs_fp64_oracle(gpu, oracle, win):
+    # the FP32 windows are evaluated with a compensated argument; against the
+    # same algorithm in FP64 every output stays within a few FP32 ulps
+    N = (16, 16, 16)
+    x, fh, f, g = case(N, 2000, 31)
+    p = gpu.Plan(N, m=6, flags=WINDOWS[win], precision="fp32")
+    o = oracle.OraclePlan(N, m=6, flags=WINDOWS[win])
+    got = p.trafo(x, fh, CF_ALL)
+    want = o.trafo(x, fh, CF_ALL)
+    for a, b, tol in zip(got, want, (2e-6, 2e-6, 5e-6)):
+        assert rel(a, b) < tol, (win, rel(a, b))
+    assert rel(p.adj(x, f, g, 1 | 2), o.adj(x, f, g, 1 | 2)) < 2e-6
 
 
 def test_accumulated_and_empty(gpu, oracle):
