@@ -76,6 +76,28 @@ int pnfft_gb300_synchronize(pnfft_plan ths);
 int pnfft_gb300_sort_nodes(pnfft_plan ths, ptrdiff_t M, const double *x, long long *pairs);
 int pnfft_gb300_node_index(pnfft_plan ths, ptrdiff_t M, const double *x, int interlaced, long long *u);
 
+/* The sort of pnfft_gb300_sort_nodes without any device allocation.  It has
+ * no counterpart in the reference; it exists for callers that cannot allocate
+ * device memory where they sort (a fixed memory pool or arena that must not
+ * grow, an allocator that forbids cudaMalloc because of its implicit
+ * synchronisation, or memory reserved in full up front).
+ *  - d_x (3M doubles) and d_pairs (2M long longs, same layout as
+ *    pnfft_gb300_sort_nodes) are device arrays of the current device; only
+ *    the plan's n and m are read.
+ *  - The scratch is one static device array of this library, sized for at
+ *    most PNFFT_GB300_SORT_NOALLOC_MAX_NODES nodes (4.5 MiB); a larger M is
+ *    refused with an error (-1).
+ *  - The first call on a device resolves the array's address on that device
+ *    (the device must be current); make it before any stream capture.
+ *  - The work is queued on cuda_stream (NULL: the legacy default stream) and
+ *    the call returns without synchronizing.
+ *  - All calls share the array: calls whose work overlaps on the GPU race and
+ *    give wrong results; order them on one stream.
+ * Returns 0 on success. */
+#define PNFFT_GB300_SORT_NOALLOC_MAX_NODES 262144
+int pnfft_gb300_sort_nodes_noalloc(const pnfft_plan ths, ptrdiff_t M, const double *d_x, long long *d_pairs,
+                                   void *cuda_stream);
+
 /* Milliseconds of the stages of the last pnfft_trafo / pnfft_adj of the plan,
  * indexed like the PNFFT_TIMER_* constants. */
 int pnfft_gb300_last_stage_ms(const pnfft_plan ths, int adjoint, double *ms10);

@@ -58,6 +58,7 @@ GB300_FP64 = 0
 GB300_FP32_MIXED = 1
 GB300_FP32 = 1 << 30
 MPI_COMM_WORLD = 0x44000000
+SORT_NOALLOC_MAX_NODES = 262144  # PNFFT_GB300_SORT_NOALLOC_MAX_NODES
 PFFT_ESTIMATE = 1 << 0
 
 _P = ctypes.c_void_p
@@ -166,6 +167,7 @@ SIGNATURES = {
     "pnfft_gb300_synchronize": (_I, [_P]),
     "pnfft_gb300_sort_nodes": (_I, [_P, _SS, _DP, _LLP]),
     "pnfft_gb300_node_index": (_I, [_P, _SS, _DP, _I, _LLP]),
+    "pnfft_gb300_sort_nodes_noalloc": (_I, [_P, _SS, _P, _P, _P]),
     "pnfft_gb300_last_stage_ms": (_I, [_P, _I, _DP]),
 }
 

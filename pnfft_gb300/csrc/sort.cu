@@ -12,7 +12,10 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <mutex>
+
 #include "pg_index.cuh"
+#include "pg_internal.h"
 #include "pg_kernels.h"
 
 namespace pg {
@@ -171,4 +174,117 @@ int radix_sort_nodes(const double *x, int64_t M, const int *n, int m, long long 
   return 0;
 }
 
+// ---------------------------------------------------------------------------
+// The node sort without any device allocation.
+//
+// Some callers cannot allocate device memory at the point where they sort:
+// code running under a device memory pool or arena that it must not grow, an
+// allocator hook that forbids cudaMalloc/cudaMallocAsync (their implicit
+// synchronisation or pool growth would stall a latency-bound loop), or a
+// process whose device memory is fully reserved up front.  For them the sort
+// below takes its scratch -- the ping-pong copy of the (key, index) pairs and
+// the per-block digit histograms -- from one statically sized device array
+// instead of cudaMallocAsync.  The array is part of this module's device
+// image and exists once per device; its address is resolved with
+// cudaGetSymbolAddress on the first call made on each device (with that
+// device current), so make one call on a device before any stream capture on
+// it.  The array holds at most kNoAllocMaxNodes nodes; larger calls are
+// refused with an error and must use the allocating sort.
+//
+// Every call shares the array and finds the previous call's contents in it.
+// Nothing there has to start at zero: every radix pass writes each digit
+// count of every block (k_radix_hist) and each of the M pairs (the stable
+// scatter is a permutation) before reading them.  Calls whose work overlaps
+// on the GPU (different streams, or threads on the same device without
+// ordering) race on the array and give wrong results; order them on one
+// stream or synchronize between them.
+// ---------------------------------------------------------------------------
+constexpr int64_t kNoAllocMaxNodes = int64_t(1) << 18;
+constexpr int kNoAllocMaxBlocks = (int)(kNoAllocMaxNodes / kBlockItems);
+constexpr size_t kNoAllocPairBytes = sizeof(long long) * 2 * (size_t)kNoAllocMaxNodes;  // 4 MiB
+constexpr size_t kNoAllocHistBytes = sizeof(int) * (size_t)kDigits * kNoAllocMaxBlocks;  // 512 KiB
+static __device__ __align__(256) unsigned char g_sort_scratch[kNoAllocPairBytes + kNoAllocHistBytes];
+
+static_assert(kNoAllocPairBytes % 256 == 0, "histograms start 256-byte aligned");
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_scratch_mu;
+static void *g_scratch_ptr[kNoAllocMaxDevices] = {};
+
+static int sort_scratch_address(void **out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_error("pnfft_gb300_sort_nodes_noalloc: cudaGetDevice failed: %s", cudaGetErrorString(e));
+    return -1;
+  }
+  if (dev < 0 || dev >= kNoAllocMaxDevices) {
+    set_error("pnfft_gb300_sort_nodes_noalloc: device %d is beyond the %d devices supported", dev, kNoAllocMaxDevices);
+    return -1;
+  }
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[dev]) {
+    void *ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_sort_scratch);
+    if (e != cudaSuccess || !ptr) {
+      set_error("pnfft_gb300_sort_nodes_noalloc: cudaGetSymbolAddress of the scratch array failed on device %d: %s",
+                dev, cudaGetErrorString(e));
+      return -1;
+    }
+    g_scratch_ptr[dev] = ptr;
+  }
+  *out = g_scratch_ptr[dev];
+  return 0;
+}
+
 }  // namespace pg
+
+extern "C" int pnfft_gb300_sort_nodes_noalloc(const pnfft_plan ths, ptrdiff_t M, const double *d_x, long long *d_pairs,
+                                              void *cuda_stream) {
+  using namespace pg;
+  if (!ths) {
+    set_error("pnfft_gb300_sort_nodes_noalloc: plan is NULL");
+    return -1;
+  }
+  if (M < 0 || M > kNoAllocMaxNodes) {
+    set_error("pnfft_gb300_sort_nodes_noalloc: M=%td is outside [0, %lld], the capacity of the static scratch; "
+              "use pnfft_gb300_sort_nodes for larger node sets",
+              M, (long long)kNoAllocMaxNodes);
+    return -1;
+  }
+  if (M == 0) return 0;
+  if (!d_x || !d_pairs) {
+    set_error("pnfft_gb300_sort_nodes_noalloc: d_x and d_pairs must be device arrays");
+    return -1;
+  }
+  void *scratch = nullptr;
+  if (sort_scratch_address(&scratch)) return -1;
+  cudaStream_t s = (cudaStream_t)cuda_stream;
+  long long *tmp = (long long *)scratch;
+  int *hist = (int *)((unsigned char *)scratch + kNoAllocPairBytes);
+  const int n0 = (int)ths->n[0], n1 = (int)ths->n[1], n2 = (int)ths->n[2];
+  k_sort_keys<<<(unsigned)((M + 255) / 256), 256, 0, s>>>(d_x, M, n0, n1, n2, ths->m, d_pairs);
+  const double nprod = (double)n0 * (double)n1 * (double)n2;
+  long long rhigh = (long long)ceil(log2(nprod)) - 1;
+  const int nblocks = (int)((M + kBlockItems - 1) / kBlockItems);
+  long long *from = d_pairs, *to = tmp;
+  int shift = 0;
+  while (rhigh >= 0) {
+    k_radix_hist<<<nblocks, 256, 0, s>>>(from, M, shift, nblocks, hist);
+    k_radix_scan<<<1, 1024, 0, s>>>(hist, (int64_t)kDigits * nblocks);
+    k_radix_scatter<<<nblocks, 32, 0, s>>>(from, to, M, shift, nblocks, hist);
+    long long *t = from;
+    from = to;
+    to = t;
+    shift += 9;
+    rhigh -= 9;
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && from != d_pairs)
+    e = cudaMemcpyAsync(d_pairs, from, sizeof(long long) * 2 * M, cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) {
+    set_error("pnfft_gb300_sort_nodes_noalloc: launch failed: %s", cudaGetErrorString(e));
+    return -1;
+  }
+  return 0;
+}
