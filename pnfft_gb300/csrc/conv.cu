@@ -112,7 +112,8 @@ __global__ void k_bin_keys(const double *__restrict__ x, int64_t M, int n0, int 
   }
   const int t0 = u[0] / b.T[0], t1 = u[1] / b.T[1], t2 = u[2] / b.T[2];
   const int tile = (t0 * b.ntile[1] + t1) * b.ntile[2] + t2;
-  const int opk = (u[0] - t0 * b.T[0]) | ((u[1] - t1 * b.T[1]) << 8) | ((u[2] - t2 * b.T[2]) << 16);
+  const int z = b.line_mode ? u[2] : u[2] - t2 * b.T[2];
+  const int opk = (u[0] - t0 * b.T[0]) | ((u[1] - t1 * b.T[1]) << 8) | (z << 16);
   b.key[j] = tile;
   store_rec(rec_unsorted, j, dist, opk, T(0));
   atomicAdd(&b.count[tile], 1);
@@ -251,6 +252,24 @@ __global__ void k_bin_subs(Binning b) {
   }
 }
 
+// line mode: one sub-problem list over lines of tiles along axis 2 (thread per line)
+__global__ void k_bin_line_subs(Binning b, int64_t M) {
+  const int nlines = b.ntile[0] * b.ntile[1];
+  const int L = blockIdx.x * blockDim.x + threadIdx.x;
+  if (L >= nlines) return;
+  const int first = b.start[L * b.ntile[2]];
+  const int end = (L + 1 < nlines) ? b.start[(L + 1) * b.ntile[2]] : (int)M;
+  const int cnt = end - first;
+  if (cnt <= 0) return;
+  const int ns = (cnt + b.sub_max - 1) / b.sub_max;
+  const int off = atomicAdd(b.nsub, ns);
+  for (int i = 0; i < ns; i++) {
+    b.sub_tile[off + i] = L;
+    b.sub_first[off + i] = first + i * b.sub_max;
+    b.sub_cnt[off + i] = min(b.sub_max, cnt - i * b.sub_max);
+  }
+}
+
 void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s) {
   const Binning &b = a.bin;
   cudaMemsetAsync(b.count, 0, sizeof(int) * b.ntiles, s);
@@ -270,7 +289,13 @@ void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s) {
     if (fp32) k_bin_scatter<float><<<bl, th, 0, s>>>(a.M, b, b.rec_tmp);
     else k_bin_scatter<double><<<bl, th, 0, s>>>(a.M, b, b.rec_tmp);
   }
-  k_bin_subs<<<(b.ntiles + 255) / 256, 256, 0, s>>>(b);
+  if (b.line_mode) {
+    const int nlines = b.ntile[0] * b.ntile[1];
+    cudaMemsetAsync(b.nsub, 0, sizeof(int), s);
+    k_bin_line_subs<<<(nlines + 255) / 256, 256, 0, s>>>(b, a.M);
+  } else {
+    k_bin_subs<<<(b.ntiles + 255) / 256, 256, 0, s>>>(b);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -953,15 +978,236 @@ __global__ void k_spread_generic(ConvArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+// spreading B^T along lines of tiles.  One CTA takes the nodes of one line
+// of 4x4x4-cell tiles running along axis 2 (the sort keeps them consecutive
+// and in slab order, slab = u2/4), or a run of at most sub_max of them.
+// Thread (a, b) owns one column of the (3+cut)^2 region in axes 0, 1 and
+// keeps W = 3+cut consecutive z values of it in registers, aligned to the
+// slab of the current node; the node's z window row (cut values at offset
+// u2 mod 4, zero elsewhere) is staged per node, so the update is a
+// branch-free W-long FMA run:
+//   acc[z] += f psi_x[a-o0] psi_y[b-o1] * psi_z[z-o2]
+// When a node lies in a later slab the window slides: its first 4 values
+// are final for this CTA and are committed with vector atomics (zeros are
+// skipped).  Each z value of a column is therefore committed once per line
+// rather than once per tile.  A complete flush after kFlushNodes nodes bounds
+// the FP32 summation length in dense clusters (the count restarts whenever
+// the window slides, so uniform nodes never trigger it).
+// ---------------------------------------------------------------------------
+template <int CUT>
+struct LineGeom {
+  static constexpr int TL = 4;                   // tile edge in every axis
+  static constexpr int R = TL + CUT - 1;         // region edge in axes 0, 1
+  static constexpr int W = TL + CUT - 1;         // z window (even)
+  static constexpr int WP = (W + 3) / 4 * 4;     // padded z row
+  static constexpr int CP = (CUT + 3) / 4 * 4;   // padded x / y rows
+  static constexpr int WREC = WP + 2 * CP;
+  static constexpr int THREADS = (R * R + 31) / 32 * 32;
+};
+constexpr int kFlushNodes = 256;
+
+// adds (r0 + i i0) at z and (r1 + i i1) at z+1 of one grid column (z even)
+__device__ __forceinline__ void commit_pair(float2 *col, int z, int n2, bool vec, float r0, float i0, float r1,
+                                            float i1) {
+  if (r0 == 0.f && i0 == 0.f && r1 == 0.f && i1 == 0.f) return;
+  if (vec) {
+    atomicAdd((float4 *)(col + z % n2), make_float4(r0, i0, r1, i1));
+  } else {
+    if (r0 != 0.f || i0 != 0.f) atomicAdd(col + z % n2, make_float2(r0, i0));
+    if (r1 != 0.f || i1 != 0.f) atomicAdd(col + (z + 1) % n2, make_float2(r1, i1));
+  }
+}
+__device__ __forceinline__ void commit_pair(double2 *col, int z, int n2, bool, double r0, double i0, double r1,
+                                            double i1) {
+  if (r0 != 0.0 || i0 != 0.0) atomic_add_grid(col + z % n2, make_double2(r0, i0));
+  if (r1 != 0.0 || i1 != 0.0) atomic_add_grid(col + (z + 1) % n2, make_double2(r1, i1));
+}
+
+template <typename T, int CUT, int MODE>
+__global__ void __launch_bounds__(LineGeom<CUT>::THREADS) k_spread_line(ConvArgs a) {
+  typedef typename Cplx<T>::type C;
+  typedef LineGeom<CUT> G;
+  constexpr int TL = G::TL, R = G::R, W = G::W, WP = G::WP, CP = G::CP, WREC = G::WREC;
+  constexpr bool DF = (MODE & 1) != 0, DG = (MODE & 2) != 0;
+  constexpr int NDER = DG ? 1 : 0;
+  constexpr int NB = sizeof(T) == 4 ? 64 : 32;  // nodes per batch
+  constexpr int WSZ = (DG ? 2 : 1) * WREC;
+  // per node: [pz (WP)][px (CP)][py (CP)] and, with DG, the same for the derivatives
+  __shared__ __align__(16) T s_w[NB][WSZ];
+  __shared__ T s_v[NB][8];  // f re/im, g0..g2 re/im (scaled)
+  __shared__ T s_d[NB][3];
+  __shared__ int s_o[NB];
+  const Binning &b = a.bin;
+  const int sub = blockIdx.x;
+  if (sub >= *b.nsub) return;
+  const int line = b.sub_tile[sub], first = b.sub_first[sub], cnt = b.sub_cnt[sub];
+  const int t1 = line % b.ntile[1], t0 = line / b.ntile[1];
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const bool active = tid < R * R;
+  const int ca = active ? tid / R : 0, cb = active ? tid % R : 0;
+  const int n0 = a.w.n[0], n1 = a.w.n[1], n2 = a.w.n[2];
+  C *col = (C *)a.grid + ((size_t)((t0 * TL + ca) % n0) * n1 + (t1 * TL + cb) % n1) * n2;
+  const bool vec = (n2 & 1) == 0;
+  T acc_r[W], acc_i[W];
+#pragma unroll
+  for (int z = 0; z < W; z++) acc_r[z] = acc_i[z] = (T)0;
+  int zslab = -1, since = 0;
+  const T scale = a.use_il ? (T)0.5 : (T)1;
+  for (int b0 = 0; b0 < cnt; b0 += NB) {
+    const int nb = min(NB, cnt - b0);
+    __syncthreads();
+    // --- stage node data and clear the z rows ---------------------------------
+    for (int i = tid; i < nb; i += nth) {
+      const int q = first + b0 + i;
+      T d[3];
+      int pk;
+      load_rec_raw(b.rec, q, d, &pk);
+      s_d[i][0] = d[0];
+      s_d[i][1] = d[1];
+      s_d[i][2] = d[2];
+      s_o[i] = pk;
+      const int64_t ind = (int64_t)b.perm[q] * a.stride + a.offset;
+      T v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (DF) {
+        if (a.real_io) v[0] = (T)a.f_in[ind];
+        else {
+          double2 f = ((const double2 *)a.f_in)[ind];
+          v[0] = (T)f.x;
+          v[1] = (T)f.y;
+        }
+      }
+      if (DG) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          if (a.real_io) v[2 + 2 * c] = (T)a.grad_in[3 * ind + c];
+          else {
+            double2 g = ((const double2 *)a.grad_in)[3 * ind + c];
+            v[2 + 2 * c] = (T)g.x;
+            v[3 + 2 * c] = (T)g.y;
+          }
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 8; c++) s_v[i][c] = v[c] * scale;
+    }
+    for (int v = tid; v < nb * WP; v += nth) {
+      const int i = v / WP, z = v - i * WP;
+      s_w[i][z] = (T)0;
+      if (DG) s_w[i][WREC + z] = (T)0;
+    }
+    __syncthreads();
+    // --- window values: all threads over (node, axis, stencil point) ------------
+    for (int v = tid; v < nb * 3 * CUT; v += nth) {
+      const int i = v / (3 * CUT), e = v - i * 3 * CUT;
+      const int t = e / CUT, sidx = e - t * CUT;
+      T out[3];
+      window_point<T>(a.w, t, sidx, s_d[i][t], NDER, out);
+      const int pos = (t == 2) ? ((s_o[i] >> 16) & (TL - 1)) + sidx : WP + t * CP + sidx;
+      s_w[i][pos] = out[0];
+      if (DG) s_w[i][WREC + pos] = out[1];
+    }
+    __syncthreads();
+    // --- accumulate, sliding the z window ----------------------------------------
+    for (int i = 0; i < nb; i++) {
+      const int pk = s_o[i];
+      const int slab = (pk >> 16) / TL;
+      if (slab != zslab) {
+        if (zslab >= 0) {
+          const int steps = slab - zslab;
+          if (steps * TL >= W) {
+#pragma unroll
+            for (int z = 0; z < W; z += 2)
+              commit_pair(col, zslab * TL + z, n2, vec, acc_r[z], acc_i[z], acc_r[z + 1], acc_i[z + 1]);
+#pragma unroll
+            for (int z = 0; z < W; z++) acc_r[z] = acc_i[z] = (T)0;
+            since = 0;
+          } else {
+            for (int q = 0; q < steps; q++) {
+              const int zb = (zslab + q) * TL;
+#pragma unroll
+              for (int z = 0; z < TL; z += 2)
+                commit_pair(col, zb + z, n2, vec, acc_r[z], acc_i[z], acc_r[z + 1], acc_i[z + 1]);
+#pragma unroll
+              for (int z = 0; z < W - TL; z++) {
+                acc_r[z] = acc_r[z + TL];
+                acc_i[z] = acc_i[z + TL];
+              }
+#pragma unroll
+              for (int z = W - TL; z < W; z++) acc_r[z] = acc_i[z] = (T)0;
+            }
+          }
+        }
+        zslab = slab;
+        since = 0;
+      }
+      if (since >= kFlushNodes) {
+#pragma unroll
+        for (int z = 0; z < W; z += 2)
+          commit_pair(col, zslab * TL + z, n2, vec, acc_r[z], acc_i[z], acc_r[z + 1], acc_i[z + 1]);
+#pragma unroll
+        for (int z = 0; z < W; z++) acc_r[z] = acc_i[z] = (T)0;
+        since = 0;
+      }
+      since++;
+      const int da = ca - (pk & 0xff), db = cb - ((pk >> 8) & 0xff);
+      if (active && (unsigned)da < (unsigned)CUT && (unsigned)db < (unsigned)CUT) {
+        const T *w = s_w[i];
+        const T pxy = w[WP + da] * w[WP + CP + db];
+        T h1r = 0, h1i = 0, h2r = 0, h2i = 0;
+        if (DF) {
+          h1r = pxy * s_v[i][0];
+          h1i = pxy * s_v[i][1];
+        }
+        if (DG) {
+          const T *wd = w + WREC;
+          const T dxy = wd[WP + da] * w[WP + CP + db], xdy = w[WP + da] * wd[WP + CP + db];
+          h1r += dxy * s_v[i][2] + xdy * s_v[i][4];
+          h1i += dxy * s_v[i][3] + xdy * s_v[i][5];
+          h2r = pxy * s_v[i][6];
+          h2i = pxy * s_v[i][7];
+        }
+        T pz[WP];
+        load_row<WP>(w, pz);
+#pragma unroll
+        for (int z = 0; z < W; z++) {
+          acc_r[z] += h1r * pz[z];
+          acc_i[z] += h1i * pz[z];
+        }
+        if (DG) {
+          T dz[WP];
+          load_row<WP>(w + WREC, dz);
+#pragma unroll
+          for (int z = 0; z < W; z++) {
+            acc_r[z] += h2r * dz[z];
+            acc_i[z] += h2i * dz[z];
+          }
+        }
+      }
+    }
+  }
+  // --- commit the last window -----------------------------------------------------
+  if (!active || zslab < 0) return;
+#pragma unroll
+  for (int z = 0; z < W; z += 2)
+    commit_pair(col, zslab * TL + z, n2, vec, acc_r[z], acc_i[z], acc_r[z + 1], acc_i[z + 1]);
+}
+
+// ---------------------------------------------------------------------------
 // dispatch
 // ---------------------------------------------------------------------------
 static const int kThreads = 256;
 
-void choose_tiles(int cut, bool fp32, const int *n, int *T) {
-  // 8x8x8 cells per tile: the interpolation stages the (8+2m)^3 region in
-  // shared memory (FP64, m=7: 170 KB), the spreading keeps it in registers
-  (void)cut;
+void choose_tiles(int cut, bool fp32, bool spread, const int *n, int *T, int *line_mode) {
+  // interpolation: 8x8x8 cells per tile, the CTA stages the (8+2m)^3 region
+  // in shared memory (FP64, m=7: 170 KB).  Spreading: lines of 4x4x4-cell
+  // tiles along axis 2 (k_spread_line); the record packs u2 in 15 bits.
   (void)fp32;
+  *line_mode = 0;
+  if (spread && cut <= 15 && n[0] >= 4 && n[1] >= 4 && n[2] >= 4 && n[2] < 32768) {
+    T[0] = T[1] = T[2] = 4;
+    *line_mode = 1;
+    return;
+  }
   for (int d = 0; d < 3; d++) T[d] = n[d] >= 8 ? 8 : n[d];
 }
 
@@ -978,7 +1224,8 @@ static void run_interp_tile(const ConvArgs &a, cudaStream_t s) {
 
 template <typename T, int CUT, int MODE>
 static void run_spread_tile(const ConvArgs &a, cudaStream_t s) {
-  k_spread_cols<T, CUT, MODE><<<a.bin.max_subs, ColGeom<CUT, 8>::THREADS, 0, s>>>(a);
+  if (a.bin.line_mode) k_spread_line<T, CUT, MODE><<<a.bin.max_subs, LineGeom<CUT>::THREADS, 0, s>>>(a);
+  else k_spread_cols<T, CUT, MODE><<<a.bin.max_subs, ColGeom<CUT, 8>::THREADS, 0, s>>>(a);
 }
 
 template <typename T, int MODE>
@@ -1008,6 +1255,7 @@ static bool spread_by_cut(const ConvArgs &a, cudaStream_t s) {
 }
 
 static bool tiles_usable(const ConvArgs &a) {
+  if (a.bin.line_mode) return a.w.cut <= 15 && a.bin.T[0] == 4 && a.bin.T[1] == 4 && a.bin.T[2] == 4;
   return a.w.cut <= 15 && a.bin.T[0] == 8 && a.bin.T[1] == 8 && a.bin.T[2] == 8;
 }
 

@@ -85,7 +85,9 @@ __global__ void k_deconv_pad(DeconvArgs a) {
     bool inside = true;
     for (int t = 0; t < 3; t++) {
       int64_t nt = a.n[t];
-      long long kk = (ii[t] < nt / 2) ? ii[t] : ii[t] - nt;  // frequency of this FFT bin
+      // frequency of this FFT bin: the k = ii (mod n) inside the stored
+      // range [ks, ks + Nl) if any (for odd n, bin (n-1)/2 is +(n-1)/2)
+      long long kk = (ii[t] < a.ks[t] + a.Nl[t]) ? ii[t] : ii[t] - nt;
       if (kk < a.ks[t] || kk >= a.ks[t] + a.Nl[t]) inside = false;
       k[t] = kk;
     }
@@ -93,7 +95,7 @@ __global__ void k_deconv_pad(DeconvArgs a) {
     if (inside) {
       const double2 *fh = (const double2 *)a.fhat_in;
       double2 f = fh[fhat_index(a, k)];
-      double w = (a.inv[0][k[0] - a.ks[0]] * a.inv[1][k[1] - a.ks[1]]) * a.inv[2][k[2] - a.ks[2]];
+      double w = (a.inv[0][k[0] - a.ks[0]] * a.inv[1][k[1] - a.ks[1]]) * a.inv[2][k[2] - a.ks[2]] * a.scale;
       v = make_double2(f.x * w, f.y * w);
       if (a.interlaced) {
         double h = ((double)k[0] / (double)a.n[0] + (double)k[1] / (double)a.n[1]) + (double)k[2] / (double)a.n[2];
@@ -145,7 +147,7 @@ __global__ void k_deconv_crop_acc(DeconvArgs a) {
       sincospi(h, &sn, &cs);
       v = cmul(v, make_double2(cs, -sn));
     }
-    double w = (a.inv[0][a0] * a.inv[1][a1]) * a.inv[2][a2];
+    double w = (a.inv[0][a0] * a.inv[1][a1]) * a.inv[2][a2] * a.scale;
     double2 o = fh[idx];
     o.x += v.x * w;
     o.y += v.y * w;

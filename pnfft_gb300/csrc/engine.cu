@@ -62,13 +62,17 @@ struct DevState {
   uint64_t tables_for = ~0ull;
   double *fhat = nullptr;
   size_t fhat_cap = 0;
-  // binning scratch for the plain and the interlaced pass
-  Binning bin[2] = {};
-  int64_t bin_cap_M = 0;
-  int bin_T[3] = {0, 0, 0};
-  int bin_prec = -1;
-  uint64_t bin_uid[2] = {0, 0}, bin_ver[2] = {0, 0};
-  bool bin_valid[2] = {false, false};
+  // node binnings [interpolation | spreading][plain | interlaced pass],
+  // allocated on first use; a valid binning of fixed nodes is reused
+  struct BinSlot {
+    Binning b = {};
+    int64_t cap = 0;
+    int T[3] = {0, 0, 0};
+    int line_mode = 0;
+    int prec = -1;
+    uint64_t uid = 0, ver = 0;
+    bool valid = false;
+  } bins[2][2];
   std::vector<Stage> pending;
   std::vector<cudaEvent_t> free_ev;
 };
@@ -158,6 +162,15 @@ static int ensure_grid_fft(pnfft_plan p) {
   return 0;
 }
 
+// FP32-mixed plans return the window of axis t times 2^-k with 2^k <= psi(0)
+// (psi(0) < 2 needs no scaling); D is multiplied by 2^(k0+k1+k2).
+static int window_kscale(pnfft_plan p, int t) {
+  if (!fp32(p)) return 0;
+  double out[3];
+  window_eval<double>(p->window, p->m, (double)p->n[t], p->b[t], 0.0, (double)p->m, 0, out);
+  return (out[0] >= 2.0) ? (int)floor(log2(out[0])) : 0;
+}
+
 static int ensure_tables(pnfft_plan p) {
   DevState *d = p->dev;
   uint64_t want = (p->table_version << 1) | (uint64_t)(fp32(p) ? 1 : 0);
@@ -176,7 +189,9 @@ static int ensure_tables(pnfft_plan p) {
       const std::vector<double> &h = p->tab[der][t];
       if (h.empty()) continue;
       if (fp32(p)) {
-        std::vector<float> tmp(h.begin(), h.end());
+        std::vector<float> tmp(h.size());
+        const int ks = window_kscale(p, t);
+        for (size_t i = 0; i < h.size(); i++) tmp[i] = (float)ldexp(h[i], -ks);
         PG_CUDA(cudaMalloc(&d->tab[der][t], sizeof(float) * tmp.size()));
         PG_CUDA(cudaMemcpy(d->tab[der][t], tmp.data(), sizeof(float) * tmp.size(), cudaMemcpyHostToDevice));
       } else {
@@ -202,43 +217,45 @@ static void free_binning(Binning &b) {
   b.bsum = nullptr;
 }
 
-static int ensure_binning(pnfft_plan p, int64_t M) {
+static int ensure_binning(pnfft_plan p, int64_t M, int spread, int il) {
   DevState *d = p->dev;
+  DevState::BinSlot &sl = d->bins[spread][il];
   int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
-  int T[3];
-  choose_tiles(p->cutoff, fp32(p), n, T);
-  bool same_tiles = T[0] == d->bin_T[0] && T[1] == d->bin_T[1] && T[2] == d->bin_T[2];
-  if (same_tiles && d->bin_cap_M >= M && d->bin[0].key && d->bin_prec == p->precision) return 0;
-  int64_t cap = std::max<int64_t>(M, std::max<int64_t>(d->bin_cap_M, 1));
-  for (int ps = 0; ps < 2; ps++) {
-    Binning &b = d->bin[ps];
-    free_binning(b);
-    for (int t = 0; t < 3; t++) {
-      b.T[t] = T[t];
-      b.ntile[t] = (n[t] + T[t] - 1) / T[t];
-    }
-    b.ntiles = b.ntile[0] * b.ntile[1] * b.ntile[2];
-    b.sub_max = 1024;
-    b.max_subs = (int)(b.ntiles + cap / b.sub_max + 1);
-    PG_CUDA(cudaMalloc(&b.key, sizeof(int) * cap));
-    PG_CUDA(cudaMalloc(&b.perm, sizeof(int) * cap));
-    PG_CUDA(cudaMalloc(&b.count, sizeof(int) * b.ntiles));
-    PG_CUDA(cudaMalloc(&b.start, sizeof(int) * b.ntiles));
-    PG_CUDA(cudaMalloc(&b.cursor, sizeof(int) * b.ntiles));
-    PG_CUDA(cudaMalloc(&b.nsub_tile, sizeof(int) * b.ntiles));
-    PG_CUDA(cudaMalloc(&b.sub_off, sizeof(int) * b.ntiles));
-    PG_CUDA(cudaMalloc(&b.sub_tile, sizeof(int) * b.max_subs));
-    PG_CUDA(cudaMalloc(&b.sub_first, sizeof(int) * b.max_subs));
-    PG_CUDA(cudaMalloc(&b.sub_cnt, sizeof(int) * b.max_subs));
-    PG_CUDA(cudaMalloc(&b.nsub, sizeof(int)));
-    PG_CUDA(cudaMalloc(&b.rec, (fp32(p) ? sizeof(float4) : sizeof(double4)) * cap));
-    PG_CUDA(cudaMalloc(&b.rec_tmp, (fp32(p) ? sizeof(float4) : sizeof(double4)) * cap));
-    PG_CUDA(cudaMalloc(&b.bsum, sizeof(int) * 2 * ((b.ntiles + 2047) / 2048 + 1)));
-    d->bin_valid[ps] = false;
+  int T[3], line_mode = 0;
+  choose_tiles(p->cutoff, fp32(p), spread != 0, n, T, &line_mode);
+  bool same = T[0] == sl.T[0] && T[1] == sl.T[1] && T[2] == sl.T[2] && line_mode == sl.line_mode;
+  if (same && sl.cap >= M && sl.b.key && sl.prec == p->precision) return 0;
+  int64_t cap = std::max<int64_t>(M, std::max<int64_t>(sl.cap, 1));
+  Binning &b = sl.b;
+  free_binning(b);
+  for (int t = 0; t < 3; t++) {
+    b.T[t] = T[t];
+    b.ntile[t] = (n[t] + T[t] - 1) / T[t];
   }
-  d->bin_cap_M = cap;
-  d->bin_prec = p->precision;
-  for (int t = 0; t < 3; t++) d->bin_T[t] = T[t];
+  b.ntiles = b.ntile[0] * b.ntile[1] * b.ntile[2];
+  b.line_mode = line_mode;
+  b.sub_max = line_mode ? 2048 : 1024;
+  const int units = line_mode ? b.ntile[0] * b.ntile[1] : b.ntiles;
+  b.max_subs = (int)(units + cap / b.sub_max + 1);
+  PG_CUDA(cudaMalloc(&b.key, sizeof(int) * cap));
+  PG_CUDA(cudaMalloc(&b.perm, sizeof(int) * cap));
+  PG_CUDA(cudaMalloc(&b.count, sizeof(int) * b.ntiles));
+  PG_CUDA(cudaMalloc(&b.start, sizeof(int) * b.ntiles));
+  PG_CUDA(cudaMalloc(&b.cursor, sizeof(int) * b.ntiles));
+  PG_CUDA(cudaMalloc(&b.nsub_tile, sizeof(int) * b.ntiles));
+  PG_CUDA(cudaMalloc(&b.sub_off, sizeof(int) * b.ntiles));
+  PG_CUDA(cudaMalloc(&b.sub_tile, sizeof(int) * b.max_subs));
+  PG_CUDA(cudaMalloc(&b.sub_first, sizeof(int) * b.max_subs));
+  PG_CUDA(cudaMalloc(&b.sub_cnt, sizeof(int) * b.max_subs));
+  PG_CUDA(cudaMalloc(&b.nsub, sizeof(int)));
+  PG_CUDA(cudaMalloc(&b.rec, (fp32(p) ? sizeof(float4) : sizeof(double4)) * cap));
+  PG_CUDA(cudaMalloc(&b.rec_tmp, (fp32(p) ? sizeof(float4) : sizeof(double4)) * cap));
+  PG_CUDA(cudaMalloc(&b.bsum, sizeof(int) * 2 * ((b.ntiles + 2047) / 2048 + 1)));
+  sl.valid = false;
+  sl.cap = cap;
+  sl.prec = p->precision;
+  sl.line_mode = line_mode;
+  for (int t = 0; t < 3; t++) sl.T[t] = T[t];
   return 0;
 }
 
@@ -340,6 +357,8 @@ static WindowArgs window_args(pnfft_plan p) {
     c.pb = (float)pb;
     c.pb_lo = (float)(pb - (double)c.pb);
     c.gnorm = (b > 0.0) ? (float)(1.0 / sqrt(kPi * b)) : 0.f;
+    c.kscale = window_kscale(p, t);
+    c.wsc = ldexpf(1.f, -c.kscale);
   }
   w.intpol_order = p->intpol_order;
   w.intpol_K = (int)p->intpol_K;
@@ -361,6 +380,7 @@ static DeconvArgs deconv_args(pnfft_plan p) {
   a.transposed = (p->pnfft_flags & PNFFT_TRANSPOSED_F_HAT) ? 1 : 0;
   a.c2r = p->c2r;
   a.grid = p->dev->grid;
+  a.scale = ldexp(1.0, window_kscale(p, 0) + window_kscale(p, 1) + window_kscale(p, 2));
   return a;
 }
 
@@ -374,14 +394,16 @@ static int fft_exec(pnfft_plan p, int direction) {
 // bins the nodes for pass `il` unless a valid binning of the same fixed nodes exists
 static int do_binning(pnfft_plan p, pnfft_nodes nd, ConvArgs &a, int il, int adj) {
   DevState *d = p->dev;
-  a.bin = d->bin[il];
-  bool reuse = nd->fixed && d->bin_valid[il] && d->bin_uid[il] == nd->uid && d->bin_ver[il] == nd->version;
+  if (ensure_binning(p, nd->local_M, adj, il)) return -1;
+  DevState::BinSlot &sl = d->bins[adj][il];
+  a.bin = sl.b;
+  bool reuse = nd->fixed && sl.valid && sl.uid == nd->uid && sl.ver == nd->version;
   if (!reuse) {
     StageScope sc(d, PNFFT_TIMER_SORT_NODES, adj);
     bin_nodes(a, fp32(p), d->stream);
-    d->bin_valid[il] = true;
-    d->bin_uid[il] = nd->uid;
-    d->bin_ver[il] = nd->version;
+    sl.valid = true;
+    sl.uid = nd->uid;
+    sl.ver = nd->version;
   }
   return 0;
 }
@@ -487,7 +509,6 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
   cudaStream_t s = d->stream;
   if (ensure_grid_fft(p) || ensure_tables(p)) return -1;
   int64_t M = nd ? nd->local_M : 0;
-  if (ensure_binning(p, M)) return -1;
   const int tuple = p->c2r ? 1 : 2;
   Arrays A;
   bool zc = false;
@@ -546,7 +567,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
         ca.il = il;
         ca.accum = (pass > 0 || (cflags & PNFFT_COMPUTE_ACCUMULATED)) ? 1 : 0;
         da.interlaced = il;
-        if (nd && !(cflags & PNFFT_OMIT_CONV)) do_binning(p, nd, ca, il, 0);
+        if (nd && !(cflags & PNFFT_OMIT_CONV) && do_binning(p, nd, ca, il, 0)) return -1;
         auto one = [&](int ikmode, int ikdim, double *out, int64_t off, int64_t stride, int mode) -> int {
           {
             StageScope sc(d, PNFFT_TIMER_MATRIX_D, 0);
@@ -632,7 +653,6 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
   cudaStream_t s = d->stream;
   if (ensure_grid_fft(p) || ensure_tables(p)) return -1;
   int64_t M = nd ? nd->local_M : 0;
-  if (ensure_binning(p, M)) return -1;
   Arrays A;
   bool zc = false;
   size_t fb = sizeof(double) * 2 * (size_t)p->local_N_total;
@@ -681,7 +701,7 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
         ca.use_il = il_plan ? 1 : 0;
         ca.il = il;
         da.interlaced = il;
-        if (nd && !(cflags & PNFFT_OMIT_CONV)) do_binning(p, nd, ca, il, 1);
+        if (nd && !(cflags & PNFFT_OMIT_CONV) && do_binning(p, nd, ca, il, 1)) return -1;
         auto one = [&](int ikmode, int ikdim, const double *fin, const double *gin, int64_t off, int64_t stride,
                        int mode) -> int {
           {
@@ -766,7 +786,8 @@ void engine_release_plan(pnfft_plan p) {
       for (int t = 0; t < 3; t++)
         if (d->tab[a][t]) cudaFree(d->tab[a][t]);
     if (d->fhat) cudaFree(d->fhat);
-    for (int ps = 0; ps < 2; ps++) free_binning(d->bin[ps]);
+    for (auto &row : d->bins)
+      for (auto &sl : row) free_binning(sl.b);
     for (cudaEvent_t e : d->free_ev) cudaEventDestroy(e);
     if (d->own) cudaStreamDestroy(d->own);
     cudaGetLastError();

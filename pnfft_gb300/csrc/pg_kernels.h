@@ -23,10 +23,14 @@ struct WindowArgs {
 
 // Node binning onto grid tiles (one tile = T0 x T1 x T2 cells of lowest
 // stencil index).  A sub-problem is a run of at most `sub_max` nodes of one
-// tile; one CTA handles one sub-problem.
+// tile; one CTA handles one sub-problem.  In line mode a sub-problem is a run
+// of the nodes of one line of tiles along axis 2 (the tiles with the same
+// t0, t1, which the sort keeps consecutive and in slab order), and the
+// records carry the full lowest z index u2 instead of the in-tile offset.
 struct Binning {
   int T[3], ntile[3];
   int ntiles, sub_max, max_subs;
+  int line_mode;
   int *key;        // [M] tile of each node
   int *perm;       // [M] nodes sorted by tile
   int *count;      // [ntiles]
@@ -67,7 +71,9 @@ struct ConvArgs {
 void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s);
 void launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
 void launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
-void choose_tiles(int cut, bool fp32, const int *n, int *T);
+// Tile shape of the binning for interpolation (spread = false) or spreading
+// (spread = true); *line_mode is set for the line-of-tiles spreading.
+void choose_tiles(int cut, bool fp32, bool spread, const int *n, int *T, int *line_mode);
 
 // Deconvolution (deconv.cu).
 struct DeconvArgs {
@@ -75,6 +81,7 @@ struct DeconvArgs {
   int64_t Nl[3], ks[3];  // stored block of f_hat (c2r: Nl2 = N2/2+1)
   int transposed, c2r;
   const double *inv[3];  // inv_phi_hat per axis for k = ks..ks+Nl-1
+  double scale;          // power of two undoing the FP32 window scaling (1 in FP64)
   int interlaced;
   int ik;                // 0 none, 1 gradient component ik_dim, 2 Hessian component ik_dim
   int ik_dim;

@@ -224,6 +224,8 @@ struct WinF {
   float ib, ib_lo;     // 1/b
   float pb, pb_lo;     // pi/b
   float gnorm;         // 1/sqrt(pi b) (Gaussian)
+  int kscale;          // the values are returned times 2^-kscale (see below)
+  float wsc;           // 2^-kscale
 };
 
 PG_HD void two_sum_f(float a, float b, float &s, float &e) {
@@ -260,13 +262,14 @@ PG_HD float bspline_jphi(int p, int j, float phi) {
 // a_k(nu) = prod_{j=1..k} (4 nu^2 - (2j-1)^2) / (k! 8^k) (Abramowitz & Stegun
 // 9.7.1), whose terms stay below 1e-8 after nine of them at x >= 12; the
 // series would accumulate ~1e-6 relative rounding over its ~20 growing terms.
-PG_HD void bessel_i01_f(float x, float &i0, float &i1) {
+// Both are returned times 2^-k.
+PG_HD void bessel_i01_f(float x, int k, float &i0, float &i1) {
   if (x < 12.f) {
-    i0 = bessel_i0<float>(x);
-    i1 = bessel_i1<float>(x);
+    i0 = ldexpf(bessel_i0<float>(x), -k);
+    i1 = ldexpf(bessel_i1<float>(x), -k);
     return;
   }
-  const float e = expf(x) / sqrtf(2.f * 3.14159265358979f * x);
+  const float e = ldexpf(expf(x), -k) / sqrtf(2.f * 3.14159265358979f * x);
   const float ix = 1.f / (8.f * x);
   float t0 = 1.f, t1 = 1.f, s0 = 1.f, s1 = 1.f;
   for (int k = 1; k <= 9; k++) {
@@ -335,10 +338,16 @@ PG_HD void sinc_h(float a, float &h, float &hp) {
   }
 }
 
-// window values at y = k + d, derivative order up to nder (out[0..2])
+// window values at y = k + d, derivative order up to nder (out[0..2]), times
+// 2^-c.kscale.  The radial windows reach exp(b m) (~1e13 for Kaiser-Bessel at
+// m = 7), so their FP32 products psi_x psi_y psi_z would overflow and the
+// deconvolved grid values (~1/phi_hat^3) would be subnormal; the host picks
+// kscale ~ log2 psi(0) and multiplies D by the inverse power of two, which
+// is exact.  The exponentials are scaled before any derivative factor.
 PG_HD void window_eval_f(int kind, int m, const WinF &c, int k, float d, int nder, float *out) {
   const float pi = 3.14159265358979f;
   const float mm = (float)m, n = c.n;
+  float post = c.wsc;  // applied at the end unless a branch scales itself
   float yh, yl;
   two_sum_f((float)k, d, yh, yl);
   const float y = yh;  // for the multiplicative factors
@@ -450,9 +459,11 @@ PG_HD void window_eval_f(int kind, int m, const WinF &c, int k, float d, int nde
         float xh, xl;
         two_prod_f(c.b, rh, xh, xl);
         xl += c.b * rl + c.b_lo * rh;
+        post = 1.f;
         if (kb) {
           // xh >= 3 here
-          const float E = expf(xh) * (1.f + xl), Ei = 1.f / E;
+          const float E0 = expf(xh) * (1.f + xl);
+          const float E = ldexpf(E0, -c.kscale), Ei = ldexpf(1.f / E0, -c.kscale);
           const float sh = 0.5f * (E - Ei), ch = 0.5f * (E + Ei);
           const float psi = sh / (pi * rh) * (1.f - rl / rh);
           out[0] = psi;
@@ -467,7 +478,7 @@ PG_HD void window_eval_f(int kind, int m, const WinF &c, int k, float d, int nde
           }
         } else {
           float i0h, i1h;
-          bessel_i01_f(xh, i0h, i1h);
+          bessel_i01_f(xh, c.kscale, i0h, i1h);
           out[0] = 0.5f * (i0h + i1h * xl);
           const float r = rh + rl;
           const float i1 = i1h + (i0h - i1h / xh) * xl;
@@ -496,6 +507,9 @@ PG_HD void window_eval_f(int kind, int m, const WinF &c, int k, float d, int nde
       break;
     }
   }
+  out[0] *= post;
+  if (nder >= 1) out[1] *= post;
+  if (nder >= 2) out[2] *= post;
 }
 
 // One-dimensional window at position x (units of [0,1)), as PNX(psi/dpsi/ddpsi)

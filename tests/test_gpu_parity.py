@@ -101,6 +101,22 @@ def test_fp64_cutoffs(gpu, oracle, m):
     assert rel(p.adj(x, f, g, 1 | 2), o.adj(x, f, g, 1 | 2)) < FP64_TOL
 
 
+@pytest.mark.parametrize("n,m", [((13, 11, 15), 3), ((18, 10, 21), 5), ((9, 12, 7), 2), ((40, 36, 66), 7)])
+def test_odd_and_wrapping_grids(gpu, oracle, n, m):
+    # odd n2 (scalar commits), n not a multiple of the tile edge, and regions
+    # that wrap over grids smaller than the stencil region
+    N = tuple(min(v, 8) for v in n)
+    x, fh, f, g = case(N, 700, 4)
+    o = oracle.OraclePlan(N, n, m=m)
+    want_t = o.trafo(x, fh, 1 | 2)
+    want_a = o.adj(x, f, g, 1 | 2)
+    for prec, tol in (("fp64", FP64_TOL), ("fp32", 3e-6)):
+        p = gpu.Plan(N, n, m=m, precision=prec)
+        got_t = p.trafo(x, fh, 1 | 2)
+        assert rel(got_t[0], want_t[0]) < tol and rel(got_t[1], want_t[1]) < tol, prec
+        assert rel(p.adj(x, f, g, 1 | 2), want_a) < tol, prec
+
+
 @pytest.mark.parametrize("win", ["kaiser_bessel", "gaussian", "bspline"])
 def test_fp64_c2r(gpu, oracle, win):
     N = (8, 12, 16)
