@@ -335,10 +335,41 @@ __device__ __forceinline__ void window_formula(const WindowArgs &w, int t, int s
   window_eval<double>(w.kind, w.m, (double)w.n[t], w.b[t], dist + (double)(w.m - s), (double)s - dist, nder, out);
 }
 
+// FP32: Horner on the fitted polynomial of stencil point s (16 FMAs per value)
+__device__ __forceinline__ float poly_eval(const float *row, float u) {
+  const float4 *r = (const float4 *)row;
+  const float4 c0 = __ldg(r), c1 = __ldg(r + 1), c2 = __ldg(r + 2), c3 = __ldg(r + 3);
+  float h = c3.w;
+  h = fmaf(h, u, c3.z);
+  h = fmaf(h, u, c3.y);
+  h = fmaf(h, u, c3.x);
+  h = fmaf(h, u, c2.w);
+  h = fmaf(h, u, c2.z);
+  h = fmaf(h, u, c2.y);
+  h = fmaf(h, u, c2.x);
+  h = fmaf(h, u, c1.w);
+  h = fmaf(h, u, c1.z);
+  h = fmaf(h, u, c1.y);
+  h = fmaf(h, u, c1.x);
+  h = fmaf(h, u, c0.w);
+  h = fmaf(h, u, c0.z);
+  h = fmaf(h, u, c0.y);
+  return fmaf(h, u, c0.x);
+}
+
 // psi (and derivatives up to nder) of stencil point s on axis t for a node at
-// fractional position dist, from the formula or the interpolation table
+// fractional position dist, from the interpolation table, the fitted
+// polynomial (FP32) or the formula
 template <typename T>
 __device__ __forceinline__ void window_point(const WindowArgs &w, int t, int s, T dist, int nder, T *out) {
+  if constexpr (sizeof(T) == 4) {
+    // the Bessel-I0 window jumps from 1/2 to 0 at y = m (s = 0, dist = 0)
+    if (w.poly && w.intpol_order < 0 && !(w.kind == WIN_BESSEL_I0 && s == 0 && dist == 0.f)) {
+      const float u = dist - 0.5f;
+      for (int d = 0; d <= nder; d++) out[d] = poly_eval(w.poly + ((d * 3 + t) * w.cut + s) * kPolyCoef, u);
+      return;
+    }
+  }
   if (w.intpol_order >= 0) {
     T dK = dist * (T)w.intpol_K;
     int k = (int)floor(dK);
@@ -442,8 +473,11 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
       s_j[i] = b.perm[first + b0 + i];
     }
     __syncthreads();
-    for (int v = tid; v < nb * 3 * CUT; v += blockDim.x) {
-      const int i = v / (3 * CUT), e = v - i * 3 * CUT;
+    // node-fastest: a warp shares one (axis, stencil point), so the fitted
+    // polynomial rows are broadcast loads
+    for (int v = tid; v < NBI * 3 * CUT; v += blockDim.x) {
+      const int e = v / NBI, i = v - e * NBI;
+      if (i >= nb) continue;
       const int t = e / CUT, sidx = e - t * CUT;
       T out[3];
       window_point<T>(a.w, t, sidx, s_d[4 * i + t], NDER, out);
@@ -592,41 +626,7 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
   }
 }
 
-// ---------------------------------------------------------------------------
-// spreading B^T, tiled, without atomics on the tile: every thread owns one
-// (a, b) column of the (8+2m)^3 region over one half of its z range and keeps
-// that piece of the region in registers.  The nodes of the sub-problem are
-// staged in batches (window values, node values, corners) by all threads;
-// then every thread adds the batch's nodes whose 13x13 (a, b) footprint
-// covers its column:
-//   acc[z] += f psi_x[a-o0] psi_y[b-o1] * psi_z[z-o2]
-// with psi_z stored zero-padded in region coordinates so that the z loop is
-// branch-free and uses vector loads.  FP32 sums are blocked and compensated:
-// each batch is summed in FP32 and folded into hi with an exact TwoSum (the
-// residual stays in acc), so rounding does not grow with the number of nodes
-// per tile (clustered nodes).  The region is committed with one global
-// atomic per non-zero grid point.
-// ---------------------------------------------------------------------------
-template <int CUT, int TT>
-struct ColGeom {
-  static constexpr int R = TT + CUT - 1;             // region edge
-  static constexpr int ZL = (R + 1) / 2;             // z values per thread
-  static constexpr int HZ = ((ZL + 3) / 4) * 4;      // padded half row
-  static constexpr int RP = 2 * HZ;                  // padded z row
-  static constexpr int XY = ((2 * CUT + 3) / 4) * 4; // px, py block
-  static constexpr int WREC = RP + XY;
-  static constexpr int THREADS = ((R * R * 2 + 31) / 32) * 32;
-};
-
-template <typename T>
-__device__ __forceinline__ void two_sum(T &hi, T &lo) {
-  T s = hi + lo;
-  T bv = s - hi;
-  T e = (hi - (s - bv)) + (lo - bv);
-  hi = s;
-  lo = e;
-}
-
+// vector loads of a staged row
 template <typename T, int N>
 __device__ __forceinline__ void load_row(const T *p, T *v);
 template <int N>
@@ -647,169 +647,6 @@ __device__ __forceinline__ void load_row(const double *p, double *v) {
     double2 t = ((const double2 *)p)[q];
     v[2 * q] = t.x;
     v[2 * q + 1] = t.y;
-  }
-}
-
-template <typename T, int CUT, int MODE>
-__global__ void __launch_bounds__(ColGeom<CUT, 8>::THREADS) k_spread_cols(ConvArgs a) {
-  typedef typename Cplx<T>::type C;
-  typedef ColGeom<CUT, 8> G;
-  constexpr int R = G::R, ZL = G::ZL, HZ = G::HZ, RP = G::RP, WREC = G::WREC;
-  constexpr bool DF = (MODE & 1) != 0, DG = (MODE & 2) != 0;
-  constexpr int NDER = DG ? 1 : 0;
-  constexpr int NB = sizeof(T) == 4 ? 32 : 16;  // nodes per batch
-  constexpr int WSZ = (DG ? 2 : 1) * WREC;
-  // per node: [pz (RP)][px (CUT)][py (CUT)][pad] and, with DG, the same for the derivatives
-  __shared__ __align__(16) T s_w[NB][WSZ];
-  __shared__ T s_v[NB][8];  // f re/im, g0..g2 re/im (already scaled)
-  __shared__ T s_d[NB][4];
-  __shared__ int s_o[NB];
-  const Binning &b = a.bin;
-  const int sub = blockIdx.x;
-  if (sub >= *b.nsub) return;
-  const int tile = b.sub_tile[sub], first = b.sub_first[sub], cnt = b.sub_cnt[sub];
-  int base[3];
-  tile_base(b, tile, base);
-  const int tid = threadIdx.x, nth = blockDim.x;
-  const int colid = tid >> 1, zh = tid & 1;
-  const bool active = colid < R * R;
-  const int ca = active ? colid / R : 0, cb = active ? colid % R : 0;
-  constexpr bool COMP = sizeof(T) == 4;
-  constexpr int ZC = COMP ? ZL : 1;
-  T acc_r[ZL], acc_i[ZL], hi_r[ZC], hi_i[ZC];
-#pragma unroll
-  for (int z = 0; z < ZL; z++) acc_r[z] = acc_i[z] = (T)0;
-#pragma unroll
-  for (int z = 0; z < ZC; z++) hi_r[z] = hi_i[z] = (T)0;
-  const T scale = a.use_il ? (T)0.5 : (T)1;
-  for (int b0 = 0; b0 < cnt; b0 += NB) {
-    const int nb = min(NB, cnt - b0);
-    __syncthreads();
-    // --- stage node data and clear the padded z rows -------------------------
-    for (int i = tid; i < nb; i += nth) {
-      const int q = first + b0 + i;
-      T d[3];
-      int pk;
-      load_rec_raw(b.rec, q, d, &pk);
-      s_d[i][0] = d[0];
-      s_d[i][1] = d[1];
-      s_d[i][2] = d[2];
-      s_o[i] = pk;
-      const int64_t ind = (int64_t)b.perm[q] * a.stride + a.offset;
-      T v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (DF) {
-        if (a.real_io) v[0] = (T)a.f_in[ind];
-        else {
-          double2 f = ((const double2 *)a.f_in)[ind];
-          v[0] = (T)f.x;
-          v[1] = (T)f.y;
-        }
-      }
-      if (DG) {
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          if (a.real_io) v[2 + 2 * c] = (T)a.grad_in[3 * ind + c];
-          else {
-            double2 g = ((const double2 *)a.grad_in)[3 * ind + c];
-            v[2 + 2 * c] = (T)g.x;
-            v[3 + 2 * c] = (T)g.y;
-          }
-        }
-      }
-#pragma unroll
-      for (int c = 0; c < 8; c++) s_v[i][c] = v[c] * scale;
-    }
-    for (int v = tid; v < nb * RP; v += nth) {
-      const int i = v / RP, z = v - i * RP;
-      s_w[i][z] = (T)0;
-      if (DG) s_w[i][WREC + z] = (T)0;
-    }
-    __syncthreads();
-    // --- window values: all threads over (node, axis, stencil point) ----------
-    for (int v = tid; v < nb * 3 * CUT; v += nth) {
-      const int i = v / (3 * CUT), e = v - i * 3 * CUT;
-      const int t = e / CUT, sidx = e - t * CUT;
-      T out[3];
-      window_point<T>(a.w, t, sidx, s_d[i][t], NDER, out);
-      int pos;
-      if (t < 2) {
-        pos = RP + t * CUT + sidx;
-      } else {
-        const int z = ((s_o[i] >> 16) & 0xff) + sidx;  // region z of this stencil point
-        pos = (z < ZL) ? z : HZ + (z - ZL);
-      }
-      s_w[i][pos] = out[0];
-      if (DG) s_w[i][WREC + pos] = out[1];
-    }
-    __syncthreads();
-    // --- accumulate the batch, then fold into hi -------------------------------
-    if (active) {
-      for (int i = 0; i < nb; i++) {
-        const int pk = s_o[i];
-        const int da = ca - (pk & 0xff), db = cb - ((pk >> 8) & 0xff);
-        if ((unsigned)da < (unsigned)CUT && (unsigned)db < (unsigned)CUT) {
-          const T *w = s_w[i];
-          const T pxy = w[RP + da] * w[RP + CUT + db];
-          T h1r = 0, h1i = 0, h2r = 0, h2i = 0;
-          if (DF) {
-            h1r = pxy * s_v[i][0];
-            h1i = pxy * s_v[i][1];
-          }
-          if (DG) {
-            const T *wd = w + WREC;
-            const T dxy = wd[RP + da] * w[RP + CUT + db], xdy = w[RP + da] * wd[RP + CUT + db];
-            h1r += dxy * s_v[i][2] + xdy * s_v[i][4];
-            h1i += dxy * s_v[i][3] + xdy * s_v[i][5];
-            h2r = pxy * s_v[i][6];
-            h2i = pxy * s_v[i][7];
-          }
-          T pz[HZ];
-          load_row<HZ>(w + zh * HZ, pz);
-#pragma unroll
-          for (int z = 0; z < ZL; z++) {
-            acc_r[z] += h1r * pz[z];
-            acc_i[z] += h1i * pz[z];
-          }
-          if (DG) {
-            T dz[HZ];
-            load_row<HZ>(w + WREC + zh * HZ, dz);
-#pragma unroll
-            for (int z = 0; z < ZL; z++) {
-              acc_r[z] += h2r * dz[z];
-              acc_i[z] += h2i * dz[z];
-            }
-          }
-        }
-      }
-      if (COMP) {
-#pragma unroll
-        for (int z = 0; z < ZC; z++) {
-          two_sum(hi_r[z], acc_r[z]);
-          two_sum(hi_i[z], acc_i[z]);
-        }
-      }
-    }
-  }
-  // --- commit the region ---------------------------------------------------------
-  if (!active) return;
-  const int n0 = a.w.n[0], n1 = a.w.n[1], n2 = a.w.n[2];
-  const int g0 = (base[0] + ca) % n0, g1 = (base[1] + cb) % n1;
-  C *grid = (C *)a.grid + ((size_t)g0 * n1 + g1) * n2;
-  const int z0 = zh * ZL;
-#pragma unroll
-  for (int z = 0; z < ZL; z++) {
-    const int zz = z0 + z;
-    if (zz >= R) break;
-    C v;
-    if (COMP) {
-      v.x = hi_r[z < ZC ? z : 0] + acc_r[z];
-      v.y = hi_i[z < ZC ? z : 0] + acc_i[z];
-    } else {
-      v.x = acc_r[z];
-      v.y = acc_i[z];
-    }
-    if (v.x == (T)0 && v.y == (T)0) continue;
-    atomic_add_grid(&grid[(base[2] + zz) % n2], v);
   }
 }
 
@@ -1031,7 +868,8 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS) k_spread_line(ConvArgs
   constexpr bool DF = (MODE & 1) != 0, DG = (MODE & 2) != 0;
   constexpr int NDER = DG ? 1 : 0;
   constexpr int NB = sizeof(T) == 4 ? 64 : 32;  // nodes per batch
-  constexpr int WSZ = (DG ? 2 : 1) * WREC;
+  constexpr int WSZ0 = (DG ? 2 : 1) * WREC;
+  constexpr int WSZ = (WSZ0 * sizeof(T) / 16) % 2 ? WSZ0 : WSZ0 + 16 / (int)sizeof(T);
   // per node: [pz (WP)][px (CP)][py (CP)] and, with DG, the same for the derivatives
   __shared__ __align__(16) T s_w[NB][WSZ];
   __shared__ T s_v[NB][8];  // f re/im, g0..g2 re/im (scaled)
@@ -1097,8 +935,11 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS) k_spread_line(ConvArgs
     }
     __syncthreads();
     // --- window values: all threads over (node, axis, stencil point) ------------
-    for (int v = tid; v < nb * 3 * CUT; v += nth) {
-      const int i = v / (3 * CUT), e = v - i * 3 * CUT;
+    // node-fastest (broadcast polynomial rows); the odd row stride in 16-byte
+    // units keeps these stores to at most 4-way bank conflicts
+    for (int v = tid; v < NB * 3 * CUT; v += nth) {
+      const int e = v / NB, i = v - e * NB;
+      if (i >= nb) continue;
       const int t = e / CUT, sidx = e - t * CUT;
       T out[3];
       window_point<T>(a.w, t, sidx, s_d[i][t], NDER, out);
@@ -1224,8 +1065,7 @@ static void run_interp_tile(const ConvArgs &a, cudaStream_t s) {
 
 template <typename T, int CUT, int MODE>
 static void run_spread_tile(const ConvArgs &a, cudaStream_t s) {
-  if (a.bin.line_mode) k_spread_line<T, CUT, MODE><<<a.bin.max_subs, LineGeom<CUT>::THREADS, 0, s>>>(a);
-  else k_spread_cols<T, CUT, MODE><<<a.bin.max_subs, ColGeom<CUT, 8>::THREADS, 0, s>>>(a);
+  k_spread_line<T, CUT, MODE><<<a.bin.max_subs, LineGeom<CUT>::THREADS, 0, s>>>(a);
 }
 
 template <typename T, int MODE>
@@ -1254,6 +1094,7 @@ static bool spread_by_cut(const ConvArgs &a, cudaStream_t s) {
   }
 }
 
+// interpolation: 8x8x8 tiles; spreading: lines of 4x4x4 tiles
 static bool tiles_usable(const ConvArgs &a) {
   if (a.bin.line_mode) return a.w.cut <= 15 && a.bin.T[0] == 4 && a.bin.T[1] == 4 && a.bin.T[2] == 4;
   return a.w.cut <= 15 && a.bin.T[0] == 8 && a.bin.T[1] == 8 && a.bin.T[2] == 8;
@@ -1263,7 +1104,7 @@ template <typename T>
 static void interp_t(const ConvArgs &a, int mode, cudaStream_t s) {
   if (a.M == 0) return;
   bool done = false;
-  if (tiles_usable(a)) {
+  if (!a.bin.line_mode && tiles_usable(a)) {
     switch (mode) {
       case 1: done = interp_by_cut<T, 1>(a, s); break;
       case 2: done = interp_by_cut<T, 2>(a, s); break;
@@ -1287,7 +1128,7 @@ template <typename T>
 static void spread_t(const ConvArgs &a, int mode, cudaStream_t s) {
   if (a.M == 0) return;
   bool done = false;
-  if (tiles_usable(a)) {
+  if (a.bin.line_mode && tiles_usable(a)) {
     switch (mode) {
       case 1: done = spread_by_cut<T, 1>(a, s); break;
       case 2: done = spread_by_cut<T, 2>(a, s); break;
