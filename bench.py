@@ -188,12 +188,14 @@ def run_gpu(args):
     work_stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(work_stream)  # all library and torch work on one stream
 
-    def device_steps(plan, K, W, fixed=False):
+    def device_steps(plan, K, W, fixed=False, tflags=None):
+        tflags = P.COMPUTE_F if tflags is None else tflags
         out_f = torch.empty(M, dtype=torch.complex128, device=dev)
+        out_g = torch.empty(M, 3, dtype=torch.complex128, device=dev) if tflags & P.COMPUTE_GRAD_F else None
         out_fh = torch.empty(int(np.prod(N)), dtype=torch.complex128, device=dev)
         s = torch.cuda.current_stream(dev)  # a dedicated stream, see run_gpu
         for _ in range(W):
-            plan.trafo_device(xd, fhd, P.COMPUTE_F, f=out_f, fixed_nodes=fixed)
+            plan.trafo_device(xd, fhd, tflags, f=out_f, grad=out_g, fixed_nodes=fixed)
             plan.adj_device(xd, fd, f_hat=out_fh, fixed_nodes=fixed)
         plan.synchronize()  # collect the warm-up's stage timers before the timed steps
         barrier()
@@ -203,7 +205,7 @@ def run_gpu(args):
             flush.fill_(1.0)  # L2 flush between timed steps (not timed)
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(s)
-            plan.trafo_device(xd, fhd, P.COMPUTE_F, f=out_f, fixed_nodes=fixed)
+            plan.trafo_device(xd, fhd, tflags, f=out_f, grad=out_g, fixed_nodes=fixed)
             plan.adj_device(xd, fd, f_hat=out_fh, fixed_nodes=fixed)
             b.record(s)
             evs.append((a, b))
@@ -230,6 +232,14 @@ def run_gpu(args):
     p32f = P.Plan(N, n, m=m, precision="fp32")
     ms_fixed, _, _, _ = device_steps(p32f, max(3, args.steps // 2), 2, fixed=True)
     p32f.close()
+    # the same step with COMPUTE_F | COMPUTE_GRAD_F in the trafo (analytic gradient)
+    p32g = P.Plan(N, n, m=m, precision="fp32")
+    ms_grad, _, _, _ = device_steps(p32g, max(3, args.steps // 2), 2, tflags=P.COMPUTE_F | P.COMPUTE_GRAD_F)
+    p32g.close()
+    # windows from PNFFT_PRE_CUB_PSI tables (6144 samples per cell at m=6)
+    p32t = P.Plan(N, n, m=m, flags=P.PRE_CUB_PSI, precision="fp32")
+    ms_tab, _, ftab, _ = device_steps(p32t, max(3, args.steps // 2), 2)
+    p32t.close()
 
     # --- dominant kernel roofline: interpolation B (trafo MATRIX_B) --------
     b_ms = statistics.mean(stage_b[0])
@@ -262,6 +272,8 @@ def run_gpu(args):
     fd_direct, _, _ = pd.trafo_device(xd[:sub].contiguous(), fhd, P.COMPUTE_F | P.COMPUTE_DIRECT)
     torch.cuda.synchronize()
     err_trafo = (torch.linalg.vector_norm(f32_out[:sub] - fd_direct) / torch.linalg.vector_norm(fd_direct)).item()
+
+    err_tab = (torch.linalg.vector_norm(ftab[:sub] - fd_direct) / torch.linalg.vector_norm(fd_direct)).item()
 
     # --- FP64 plain path -----------------------------------------------------
     k64 = max(1, min(3, args.steps))
@@ -315,7 +327,9 @@ def run_gpu(args):
     L.pnfft_free_nodes(nodes, P.FREE_X | P.FREE_F)
     L.pnfft_finalize(plan, P.FREE_F_HAT)
 
-    launches_per_step = 12  # bin(4)+D+B  and  bin(4)+B^T+D^T  (cuFFT kernels not counted)
+    # trafo: binning (keys, 3 scans, scatter, sub-problems) + D + B; adj: binning
+    # (keys, 3 scans, scatter, line sub-problems) + B^T + D^T (cuFFT not counted)
+    launches_per_step = 16
     line = {"metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -330,7 +344,11 @@ def run_gpu(args):
                      "err_trafo_vs_ndft": err_trafo_64},
             "accuracy": {"fp32_trafo_rel_l2_vs_fp64_ndft_4096": err_trafo, "fp32_adj_rel_l2_vs_fp64_path": err_adj},
             "amortised_fixed_nodes": {"value": M / (statistics.mean(ms_fixed) * 1e-3) / 1e6,
-                                      "ms_per_step": statistics.mean(ms_fixed)}}
+                                      "ms_per_step": statistics.mean(ms_fixed)},
+            "with_grad": {"value": M / (statistics.mean(ms_grad) * 1e-3) / 1e6,
+                          "ms_per_step": statistics.mean(ms_grad), "trafo_flags": "COMPUTE_F|COMPUTE_GRAD_F"},
+            "pre_cub_psi": {"value": M / (statistics.mean(ms_tab) * 1e-3) / 1e6,
+                            "ms_per_step": statistics.mean(ms_tab), "err_trafo_vs_ndft": err_tab}}
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in cpu_sample().items() if k != "seconds_per_step_extrapolated"}
     if rank == 0:

@@ -818,28 +818,29 @@ __global__ void k_spread_generic(ConvArgs a) {
 // spreading B^T along lines of tiles.  One CTA takes the nodes of one line
 // of 4x4x4-cell tiles running along axis 2 (the sort keeps them consecutive
 // and in slab order, slab = u2/4), or a run of at most sub_max of them.
-// Thread (a, b) owns one column of the (3+cut)^2 region in axes 0, 1 and
-// keeps W = 3+cut consecutive z values of it in registers, aligned to the
-// slab of the current node; the node's z window row (cut values at offset
-// u2 mod 4, zero elsewhere) is staged per node, so the update is a
-// branch-free W-long FMA run:
+// The (3+cut)^2 region of the line in axes 0, 1 is split into column pairs:
+// thread (a, b) owns the columns (a, b) and (a, b + R/2), and keeps W = 3+cut
+// consecutive z values of each in registers, aligned to the slab of the
+// current node.  The node's z window row (cut values at offset u2 mod 4, zero
+// elsewhere) is staged per node, so each update is a branch-free W-long FMA
+// run, and the node decode and the psi_x / psi_z loads serve both columns:
 //   acc[z] += f psi_x[a-o0] psi_y[b-o1] * psi_z[z-o2]
 // When a node lies in a later slab the window slides: its first 4 values
 // are final for this CTA and are committed with vector atomics (zeros are
 // skipped).  Each z value of a column is therefore committed once per line
-// rather than once per tile.  A complete flush after kFlushNodes nodes bounds
-// the FP32 summation length in dense clusters (the count restarts whenever
-// the window slides, so uniform nodes never trigger it).
+// rather than once per tile.  A complete flush after kFlushNodes nodes since
+// the last slide bounds the FP32 summation length in dense clusters.
 // ---------------------------------------------------------------------------
 template <int CUT>
 struct LineGeom {
   static constexpr int TL = 4;                   // tile edge in every axis
-  static constexpr int R = TL + CUT - 1;         // region edge in axes 0, 1
+  static constexpr int R = TL + CUT - 1;         // region edge in axes 0, 1 (even)
+  static constexpr int HR = R / 2;               // column pairs per region row
   static constexpr int W = TL + CUT - 1;         // z window (even)
   static constexpr int WP = (W + 3) / 4 * 4;     // padded z row
   static constexpr int CP = (CUT + 3) / 4 * 4;   // padded x / y rows
   static constexpr int WREC = WP + 2 * CP;
-  static constexpr int THREADS = (R * R + 31) / 32 * 32;
+  static constexpr int THREADS = (R * HR + 31) / 32 * 32;
 };
 constexpr int kFlushNodes = 256;
 
@@ -861,10 +862,10 @@ __device__ __forceinline__ void commit_pair(double2 *col, int z, int n2, bool, d
 }
 
 template <typename T, int CUT, int MODE>
-__global__ void __launch_bounds__(LineGeom<CUT>::THREADS) k_spread_line(ConvArgs a) {
+__global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1) k_spread_line(ConvArgs a) {
   typedef typename Cplx<T>::type C;
   typedef LineGeom<CUT> G;
-  constexpr int TL = G::TL, R = G::R, W = G::W, WP = G::WP, CP = G::CP, WREC = G::WREC;
+  constexpr int TL = G::TL, R = G::R, HR = G::HR, W = G::W, WP = G::WP, CP = G::CP, WREC = G::WREC;
   constexpr bool DF = (MODE & 1) != 0, DG = (MODE & 2) != 0;
   constexpr int NDER = DG ? 1 : 0;
   constexpr int NB = sizeof(T) == 4 ? 64 : 32;  // nodes per batch
@@ -881,16 +882,28 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS) k_spread_line(ConvArgs
   const int line = b.sub_tile[sub], first = b.sub_first[sub], cnt = b.sub_cnt[sub];
   const int t1 = line % b.ntile[1], t0 = line / b.ntile[1];
   const int tid = threadIdx.x, nth = blockDim.x;
-  const bool active = tid < R * R;
-  const int ca = active ? tid / R : 0, cb = active ? tid % R : 0;
+  const bool active = tid < R * HR;
+  const int ca = active ? tid / HR : 0, cb = active ? tid % HR : 0;
   const int n0 = a.w.n[0], n1 = a.w.n[1], n2 = a.w.n[2];
-  C *col = (C *)a.grid + ((size_t)((t0 * TL + ca) % n0) * n1 + (t1 * TL + cb) % n1) * n2;
+  const size_t gx = (size_t)((t0 * TL + ca) % n0) * n1;
+  C *col[2] = {(C *)a.grid + (gx + (t1 * TL + cb) % n1) * n2, (C *)a.grid + (gx + (t1 * TL + cb + HR) % n1) * n2};
   const bool vec = (n2 & 1) == 0;
-  T acc_r[W], acc_i[W];
+  T acc_r[2][W], acc_i[2][W];
 #pragma unroll
-  for (int z = 0; z < W; z++) acc_r[z] = acc_i[z] = (T)0;
+  for (int c = 0; c < 2; c++)
+#pragma unroll
+    for (int z = 0; z < W; z++) acc_r[c][z] = acc_i[c][z] = (T)0;
   int zslab = -1, since = 0;
   const T scale = a.use_il ? (T)0.5 : (T)1;
+  // commit values [z0, z1) of both columns at grid z = zb + z
+  auto commit = [&](int zb, int z0, int z1) {
+#pragma unroll
+    for (int c = 0; c < 2; c++)
+#pragma unroll
+      for (int z = 0; z < W; z += 2)
+        if (z >= z0 && z < z1)
+          commit_pair(col[c], zb + z, n2, vec, acc_r[c][z], acc_i[c][z], acc_r[c][z + 1], acc_i[c][z + 1]);
+  };
   for (int b0 = 0; b0 < cnt; b0 += NB) {
     const int nb = min(NB, cnt - b0);
     __syncthreads();
@@ -949,6 +962,14 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS) k_spread_line(ConvArgs
     }
     __syncthreads();
     // --- accumulate, sliding the z window ----------------------------------------
+    if (since >= kFlushNodes) {
+      commit(zslab * TL, 0, W);
+#pragma unroll
+      for (int c = 0; c < 2; c++)
+#pragma unroll
+        for (int z = 0; z < W; z++) acc_r[c][z] = acc_i[c][z] = (T)0;
+      since = 0;
+    }
     for (int i = 0; i < nb; i++) {
       const int pk = s_o[i];
       const int slab = (pk >> 16) / TL;
@@ -956,71 +977,82 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS) k_spread_line(ConvArgs
         if (zslab >= 0) {
           const int steps = slab - zslab;
           if (steps * TL >= W) {
+            commit(zslab * TL, 0, W);
 #pragma unroll
-            for (int z = 0; z < W; z += 2)
-              commit_pair(col, zslab * TL + z, n2, vec, acc_r[z], acc_i[z], acc_r[z + 1], acc_i[z + 1]);
+            for (int c = 0; c < 2; c++)
 #pragma unroll
-            for (int z = 0; z < W; z++) acc_r[z] = acc_i[z] = (T)0;
-            since = 0;
+              for (int z = 0; z < W; z++) acc_r[c][z] = acc_i[c][z] = (T)0;
           } else {
             for (int q = 0; q < steps; q++) {
-              const int zb = (zslab + q) * TL;
+              commit((zslab + q) * TL, 0, TL);
 #pragma unroll
-              for (int z = 0; z < TL; z += 2)
-                commit_pair(col, zb + z, n2, vec, acc_r[z], acc_i[z], acc_r[z + 1], acc_i[z + 1]);
+              for (int c = 0; c < 2; c++) {
 #pragma unroll
-              for (int z = 0; z < W - TL; z++) {
-                acc_r[z] = acc_r[z + TL];
-                acc_i[z] = acc_i[z + TL];
+                for (int z = 0; z < W - TL; z++) {
+                  acc_r[c][z] = acc_r[c][z + TL];
+                  acc_i[c][z] = acc_i[c][z + TL];
+                }
+#pragma unroll
+                for (int z = W - TL; z < W; z++) acc_r[c][z] = acc_i[c][z] = (T)0;
               }
-#pragma unroll
-              for (int z = W - TL; z < W; z++) acc_r[z] = acc_i[z] = (T)0;
             }
           }
         }
         zslab = slab;
         since = 0;
       }
-      if (since >= kFlushNodes) {
-#pragma unroll
-        for (int z = 0; z < W; z += 2)
-          commit_pair(col, zslab * TL + z, n2, vec, acc_r[z], acc_i[z], acc_r[z + 1], acc_i[z + 1]);
-#pragma unroll
-        for (int z = 0; z < W; z++) acc_r[z] = acc_i[z] = (T)0;
-        since = 0;
-      }
       since++;
-      const int da = ca - (pk & 0xff), db = cb - ((pk >> 8) & 0xff);
-      if (active && (unsigned)da < (unsigned)CUT && (unsigned)db < (unsigned)CUT) {
+      const int da = ca - (pk & 0xff), o1 = (pk >> 8) & 0xff;
+      const bool row = active && (unsigned)da < (unsigned)CUT;
+      const bool cov0 = row && (unsigned)(cb - o1) < (unsigned)CUT;
+      const bool cov1 = row && (unsigned)(cb + HR - o1) < (unsigned)CUT;
+      if (cov0 || cov1) {
         const T *w = s_w[i];
-        const T pxy = w[WP + da] * w[WP + CP + db];
-        T h1r = 0, h1i = 0, h2r = 0, h2i = 0;
+        const T px = w[WP + da];
+        T fr = 0, fi = 0, g0r = 0, g0i = 0, g1r = 0, g1i = 0, g2r = 0, g2i = 0, dpx = 0;
         if (DF) {
-          h1r = pxy * s_v[i][0];
-          h1i = pxy * s_v[i][1];
+          fr = px * s_v[i][0];
+          fi = px * s_v[i][1];
         }
         if (DG) {
-          const T *wd = w + WREC;
-          const T dxy = wd[WP + da] * w[WP + CP + db], xdy = w[WP + da] * wd[WP + CP + db];
-          h1r += dxy * s_v[i][2] + xdy * s_v[i][4];
-          h1i += dxy * s_v[i][3] + xdy * s_v[i][5];
-          h2r = pxy * s_v[i][6];
-          h2i = pxy * s_v[i][7];
+          dpx = w[WREC + WP + da];
+          g0r = dpx * s_v[i][2];
+          g0i = dpx * s_v[i][3];
+          g1r = px * s_v[i][4];
+          g1i = px * s_v[i][5];
+          g2r = px * s_v[i][6];
+          g2i = px * s_v[i][7];
         }
         T pz[WP];
         load_row<WP>(w, pz);
+        T dz[DG ? WP : 1];
+        if (DG) load_row<WP>(w + WREC, dz);
 #pragma unroll
-        for (int z = 0; z < W; z++) {
-          acc_r[z] += h1r * pz[z];
-          acc_i[z] += h1i * pz[z];
-        }
-        if (DG) {
-          T dz[WP];
-          load_row<WP>(w + WREC, dz);
+        for (int c = 0; c < 2; c++) {
+          const bool cov = c ? cov1 : cov0;
+          if (cov) {
+            const int db = cb + c * HR - ((pk >> 8) & 0xff);
+            const T py = w[WP + CP + db];
+            // h1 multiplies psi_z, h2 multiplies psi_z'
+            T h1r = fr * py, h1i = fi * py;
+            if (DG) {
+              const T dpy = w[WREC + WP + CP + db];
+              h1r += g0r * py + g1r * dpy;
+              h1i += g0i * py + g1i * dpy;
+            }
 #pragma unroll
-          for (int z = 0; z < W; z++) {
-            acc_r[z] += h2r * dz[z];
-            acc_i[z] += h2i * dz[z];
+            for (int z = 0; z < W; z++) {
+              acc_r[c][z] += h1r * pz[z];
+              acc_i[c][z] += h1i * pz[z];
+            }
+            if (DG) {
+              const T h2r = g2r * py, h2i = g2i * py;
+#pragma unroll
+              for (int z = 0; z < W; z++) {
+                acc_r[c][z] += h2r * dz[z];
+                acc_i[c][z] += h2i * dz[z];
+              }
+            }
           }
         }
       }
@@ -1028,9 +1060,7 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS) k_spread_line(ConvArgs
   }
   // --- commit the last window -----------------------------------------------------
   if (!active || zslab < 0) return;
-#pragma unroll
-  for (int z = 0; z < W; z += 2)
-    commit_pair(col, zslab * TL + z, n2, vec, acc_r[z], acc_i[z], acc_r[z + 1], acc_i[z + 1]);
+  commit(zslab * TL, 0, W);
 }
 
 // ---------------------------------------------------------------------------
