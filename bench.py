@@ -349,12 +349,82 @@ def run_gpu(args):
                           "ms_per_step": statistics.mean(ms_grad), "trafo_flags": "COMPUTE_F|COMPUTE_GRAD_F"},
             "pre_cub_psi": {"value": M / (statistics.mean(ms_tab) * 1e-3) / 1e6,
                             "ms_per_step": statistics.mean(ms_tab), "err_trafo_vs_ndft": err_tab}}
+    if rank == 0 and world == 1 and not args.no_batch:
+        line["batched"] = run_batched(P, torch, dev)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in cpu_sample().items() if k != "seconds_per_step_extrapolated"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def run_batched(P, torch, dev, steps=5):
+    """Config 5: 64 FP32-mixed plans of uneven size (N_t from {16..128},
+    sigma 2, M log-uniform in [1e3, 2^21], Kaiser-Bessel m = 4..6), each one
+    trafo + one adj, plus 8 right-hand sides sharing one node set of 2^20
+    nodes at N = 64^3.  One CUDA graph replays the whole batch; the eager loop
+    over the same calls is timed beside it.  Error: FP32-mixed trafo against
+    the FP64 path on 8 of the plans."""
+    from pnfft_gb300.batch import Batch
+    rng = np.random.default_rng(5)
+    sizes = [16, 32, 48, 64, 96, 128]
+    batch = Batch(dev)
+    checks = []
+    for i in range(64):
+        N = tuple(int(v) for v in rng.choice(sizes, 3))
+        M = int(round(np.exp(rng.uniform(np.log(1e3), np.log(2 ** 21)))))
+        m = int(rng.integers(4, 7))
+        p = P.Plan(N, m=m, precision="fp32")
+        x = torch.tensor(rng.uniform(-0.5, 0.5, (M, 3)), device=dev)
+        S = int(np.prod(N))
+        fh = torch.tensor(rng.standard_normal(S) + 1j * rng.standard_normal(S), device=dev)
+        fi = torch.tensor(rng.standard_normal(M) + 1j * rng.standard_normal(M), device=dev)
+        fo = torch.empty(M, dtype=torch.complex128, device=dev)
+        fho = torch.empty(S, dtype=torch.complex128, device=dev)
+        batch.add_trafo(p, x, fh, fo)
+        batch.add_adj(p, x, fi, fho)
+        if i % 8 == 0:
+            checks.append((N, m, x, fh, fo))
+    Nk, Mk = (64, 64, 64), 2 ** 20
+    pk = P.Plan(Nk, m=6, precision="fp32")
+    xk = torch.tensor(rng.uniform(-0.5, 0.5, (Mk, 3)), device=dev)
+    for _ in range(8):
+        fh = torch.tensor(rng.standard_normal(64 ** 3) + 1j * rng.standard_normal(64 ** 3), device=dev)
+        fi = torch.tensor(rng.standard_normal(Mk) + 1j * rng.standard_normal(Mk), device=dev)
+        batch.add_trafo(pk, xk, fh, torch.empty(Mk, dtype=torch.complex128, device=dev))
+        batch.add_adj(pk, xk, fi, torch.empty(64 ** 3, dtype=torch.complex128, device=dev))
+    choice = batch.autotune(reps=1)
+    batch.capture()
+
+    def timed(fn):
+        fn()
+        batch.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(batch.stream)
+        for _ in range(steps):
+            fn()
+        b.record(batch.stream)
+        b.synchronize()
+        return a.elapsed_time(b) / steps
+
+    ms_graph = timed(batch.run)
+    ms_eager = timed(batch.run_eager)
+    nodes = batch.nodes()
+    errs = []
+    for N, m, x, fh, fo in checks:
+        q = P.Plan(N, m=m, precision="fp64")
+        ref, _, _ = q.trafo_device(x, fh, P.COMPUTE_F)
+        torch.cuda.synchronize()
+        errs.append((torch.linalg.vector_norm(fo - ref) / torch.linalg.vector_norm(ref)).item())
+        q.close()
+    return {"value": nodes / (ms_graph * 1e-3) / 1e6, "unit": "Mpts/s", "ms_per_replay": ms_graph,
+            "eager_value": nodes / (ms_eager * 1e-3) / 1e6, "eager_ms": ms_eager,
+            "plans": 65, "rhs_sharing_nodes": 8, "node_transforms_per_replay": nodes,
+            "per_node_kernels_chosen": sum(1 for c in choice.values() if c[0] == 1),
+            "max_rel_err_fp32_vs_fp64_trafo": max(errs),
+            "workload": "64 plans N_t in {16..128}, M log-uniform [1e3, 2^21], KB m 4..6, trafo+adj each; "
+                        "8 RHS on one node set M=2^20 at N=64^3; one CUDA graph"}
 
 
 def run_profile_case():
@@ -378,6 +448,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-plans (CUDA graph) row")
     ap.add_argument("--profile", action="store_true",
                     help="one warm-up and one FP32-mixed trafo+adj of the workload, for ncu (no timing output)")
     args = ap.parse_args()

@@ -46,8 +46,18 @@ int pnfft_gb300_set_precision(pnfft_plan ths, int precision);
 int pnfft_gb300_get_precision(const pnfft_plan ths);
 
 /* Run the plan's work on a caller-owned cudaStream_t (NULL = the plan's own
- * stream).  Returns 0 on success. */
+ * stream).  Returns 0 on success.
+ * CUDA graphs: pnfft_trafo / pnfft_adj may be captured on that stream once
+ * one call with the same plan, node count and flags has run, if the nodes
+ * and f_hat are device arrays (below); stage timers are skipped while the
+ * stream is capturing.  Host arrays are refused during capture. */
 int pnfft_gb300_set_stream(pnfft_plan ths, void *cuda_stream);
+
+/* Convolution kernels of a plan: 0 = tiled B and line-wise B^T where the
+ * cutoff and grid allow (default), 1 = one thread per node (small node
+ * counts on large grids).  Chosen per plan, e.g. by timing both. */
+int pnfft_gb300_set_conv_method(pnfft_plan ths, int method);
+int pnfft_gb300_get_conv_method(const pnfft_plan ths);
 
 /* Zero-copy mode.  When device arrays are attached, pnfft_trafo/pnfft_adj read
  * and write them directly and return without synchronizing the stream; the

@@ -238,6 +238,10 @@ class Plan:
         L.pnfft_gb300_set_device_arrays(self._nodes, None, None, None, None)
         L.pnfft_gb300_set_device_f_hat(self._p, None)
 
+    def set_conv_method(self, method):
+        """0: tiled interpolation / line-wise spreading (default); 1: one thread per node."""
+        _check(load().pnfft_gb300_set_conv_method(self._p, int(method)), "set_conv_method")
+
     def trafo_device(self, x, f_hat, compute_flags=COMPUTE_F, f=None, grad=None, hess=None, stream=None,
                      fixed_nodes=False):
         """pnfft_trafo on CUDA tensors: x (M,3) float64, f_hat complex128 in the

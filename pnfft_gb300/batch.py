@@ -1,0 +1,122 @@
+"""Batches of transforms replayed as one CUDA graph.
+
+A batch is a list of transforms on device-resident torch tensors:
+- many plans of uneven sizes N and node counts M;
+- several right-hand sides that share one node set (the same plan and the
+  same x, different f_hat / f).
+
+``Batch`` runs every item once, eagerly, so that the first call allocates
+each plan's grid, FFT plan, window tables and node binning. The node sets
+are declared fixed, so the binning is computed once and reused. It can then
+pick each plan's convolution kernels by timing them (``autotune``: the tiled
+interpolation / line-wise spreading kernels against the one-thread-per-node
+kernels, which win for small M on large grids). Finally it captures all items
+on one stream into a single CUDA graph. ``run()`` replays the whole batch with
+one graph launch, so the per-call host work of the C library (argument
+checks, stream and pointer setup, about 50 launches per item) is paid once
+at capture.
+
+The captured graph keeps the device pointers of the items: refill the same
+tensors in place between replays.
+"""
+import torch
+
+from . import COMPUTE_F, Plan  # noqa: F401  (Plan for type references in docs)
+
+__all__ = ["Batch"]
+
+
+class Batch:
+    def __init__(self, device=None):
+        self.items = []
+        self.device = torch.device(device or "cuda")
+        self.stream = torch.cuda.Stream(self.device)
+        self.graph = None
+        self.choice = {}
+
+    # -- building -------------------------------------------------------------
+    def add_trafo(self, plan, x, f_hat, f, compute_flags=COMPUTE_F, grad=None, hess=None):
+        """f (and grad / hess) = trafo(f_hat) at nodes x, all CUDA tensors."""
+        self.items.append(("trafo", plan, x, f_hat, f, grad, hess, compute_flags))
+        self.graph = None
+
+    def add_adj(self, plan, x, f, f_hat, compute_flags=COMPUTE_F, grad=None):
+        """f_hat = adj(f) (and grad inputs with COMPUTE_GRAD_F) at nodes x."""
+        self.items.append(("adj", plan, x, f_hat, f, grad, None, compute_flags))
+        self.graph = None
+
+    def nodes(self):
+        """Total node count over the items (one trafo or adj each)."""
+        return sum(int(it[2].shape[0]) for it in self.items)
+
+    # -- execution ------------------------------------------------------------
+    def _run_item(self, it):
+        kind, plan, x, f_hat, f, grad, hess, flags = it
+        if kind == "trafo":
+            plan.trafo_device(x, f_hat, flags, f=f, grad=grad, hess=hess, fixed_nodes=True)
+        else:
+            plan.adj_device(x, f, grad, flags, f_hat=f_hat, fixed_nodes=True)
+
+    def run_eager(self):
+        """Run the items one by one on the batch stream (no graph)."""
+        with torch.cuda.stream(self.stream):
+            for it in self.items:
+                self._run_item(it)
+
+    def _time_plan(self, plan, reps):
+        items = [it for it in self.items if it[1] is plan]
+        with torch.cuda.stream(self.stream):
+            for it in items:
+                self._run_item(it)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(self.stream)
+            for _ in range(reps):
+                for it in items:
+                    self._run_item(it)
+            b.record(self.stream)
+        b.synchronize()
+        return a.elapsed_time(b) / reps
+
+    def autotune(self, reps=3):
+        """Per plan: time the tiled / line kernels (0) against the per-node
+        kernels (1) on the plan's own items and keep the faster."""
+        for p in self._plans():
+            t = {}
+            for method in (0, 1):
+                p.set_conv_method(method)
+                t[method] = self._time_plan(p, reps)
+            best = min(t, key=t.get)
+            p.set_conv_method(best)
+            self.choice[id(p)] = (best, t)
+        self.graph = None
+        return self.choice
+
+    def _plans(self):
+        plans = []
+        for it in self.items:
+            if all(it[1] is not p for p in plans):
+                plans.append(it[1])
+        return plans
+
+    def capture(self):
+        """Warm every item up, then capture all of them into one CUDA graph."""
+        self.run_eager()
+        for p in self._plans():
+            p.synchronize()  # also recycles the stage-timer events of the eager calls
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
+            for it in self.items:
+                self._run_item(it)
+        self.graph = g
+        return g
+
+    def run(self):
+        """Replay the captured batch (captures it first if needed)."""
+        if self.graph is None:
+            self.capture()
+        with torch.cuda.stream(self.stream):  # replay() launches on the current stream
+            self.graph.replay()
+
+    def synchronize(self):
+        self.stream.synchronize()

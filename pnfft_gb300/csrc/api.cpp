@@ -889,6 +889,16 @@ extern "C" int pnfft_gb300_set_precision(pnfft_plan ths, int precision) {
   return 0;
 }
 extern "C" int pnfft_gb300_get_precision(const pnfft_plan ths) { return ths ? ths->precision : -1; }
+extern "C" int pnfft_gb300_set_conv_method(pnfft_plan ths, int method) {
+  if (!ths) return -1;
+  if (method != 0 && method != 1) {
+    set_error("pnfft_gb300_set_conv_method: unknown method %d (0: tiled, 1: per node)", method);
+    return -1;
+  }
+  ths->conv_method = method;
+  return 0;
+}
+extern "C" int pnfft_gb300_get_conv_method(const pnfft_plan ths) { return ths ? ths->conv_method : -1; }
 extern "C" int pnfft_gb300_set_stream(pnfft_plan ths, void *stream) { return ths ? engine_set_stream(ths, stream) : -1; }
 extern "C" int pnfft_gb300_set_device_f_hat(pnfft_plan ths, void *d) {
   if (!ths) return -1;

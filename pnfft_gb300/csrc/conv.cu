@@ -1134,7 +1134,7 @@ template <typename T>
 static void interp_t(const ConvArgs &a, int mode, cudaStream_t s) {
   if (a.M == 0) return;
   bool done = false;
-  if (!a.bin.line_mode && tiles_usable(a)) {
+  if (!a.generic && !a.bin.line_mode && tiles_usable(a)) {
     switch (mode) {
       case 1: done = interp_by_cut<T, 1>(a, s); break;
       case 2: done = interp_by_cut<T, 2>(a, s); break;
@@ -1158,7 +1158,7 @@ template <typename T>
 static void spread_t(const ConvArgs &a, int mode, cudaStream_t s) {
   if (a.M == 0) return;
   bool done = false;
-  if (a.bin.line_mode && tiles_usable(a)) {
+  if (!a.generic && a.bin.line_mode && tiles_usable(a)) {
     switch (mode) {
       case 1: done = spread_by_cut<T, 1>(a, s); break;
       case 2: done = spread_by_cut<T, 2>(a, s); break;

@@ -75,6 +75,7 @@ struct DevState {
     bool valid = false;
   } bins[2][2];
   std::vector<Stage> pending;
+  bool capturing = false;  // the current call is being captured into a CUDA graph
   std::vector<cudaEvent_t> free_ev;
 };
 
@@ -378,6 +379,7 @@ struct StageScope {
   DevState *d;
   Stage st;
   StageScope(DevState *d_, int idx, int adj) : d(d_) {
+    if (d->capturing) return;  // no stage timers inside a captured graph
     st.idx = idx;
     st.adj = adj;
     st.a = get_event(d);
@@ -385,6 +387,7 @@ struct StageScope {
     cudaEventRecord(st.a, d->stream);
   }
   ~StageScope() {
+    if (d->capturing) return;
     cudaEventRecord(st.b, d->stream);
     d->pending.push_back(st);
   }
@@ -579,6 +582,25 @@ static int resolve_arrays(pnfft_plan p, pnfft_nodes nd, unsigned cflags, bool ad
   return 0;
 }
 
+// A call made while the plan's stream is being captured into a CUDA graph
+// must touch device memory only: every array attached with
+// pnfft_gb300_set_device_arrays / _set_device_f_hat, and the buffers already
+// allocated by an earlier call with the same sizes.  Host arrays would need
+// copies and a synchronisation, so they are refused.
+static int begin_call(pnfft_plan p, pnfft_nodes nd, const char *who) {
+  DevState *d = p->dev;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  PG_CUDA(cudaStreamIsCapturing(d->stream, &cs));
+  d->capturing = cs != cudaStreamCaptureStatusNone;
+  if (d->capturing && ((nd && !nd->u_x) || !p->d_f_hat_user)) {
+    set_error("%s: the stream is being captured into a CUDA graph; attach device arrays for the nodes and f_hat "
+              "(pnfft_gb300_set_device_arrays / pnfft_gb300_set_device_f_hat) and make one call before capturing",
+              who);
+    return -1;
+  }
+  return 0;
+}
+
 // ---------------------------------------------------------------------------
 // pnfft_trafo
 // ---------------------------------------------------------------------------
@@ -586,6 +608,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
   if (ensure_dev(p)) return -1;
   DevState *d = p->dev;
   cudaStream_t s = d->stream;
+  if (begin_call(p, nd, "pnfft_trafo")) return -1;
   if (ensure_grid_fft(p) || ensure_tables(p)) return -1;
   int64_t M = nd ? nd->local_M : 0;
   const int tuple = p->c2r ? 1 : 2;
@@ -633,6 +656,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       ConvArgs ca;
       memset(&ca, 0, sizeof(ca));
       ca.w = window_args(p);
+      ca.generic = p->conv_method == 1;
       ca.real_only = p->c2r || (p->pnfft_flags & PNFFT_PRE_QUAD_PSI) ? 1 : 0;
       ca.real_io = p->c2r;
       ca.M = M;
@@ -730,6 +754,7 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
   if (ensure_dev(p)) return -1;
   DevState *d = p->dev;
   cudaStream_t s = d->stream;
+  if (begin_call(p, nd, "pnfft_adj")) return -1;
   if (ensure_grid_fft(p) || ensure_tables(p)) return -1;
   int64_t M = nd ? nd->local_M : 0;
   Arrays A;
@@ -768,6 +793,7 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       ConvArgs ca;
       memset(&ca, 0, sizeof(ca));
       ca.w = window_args(p);
+      ca.generic = p->conv_method == 1;
       ca.real_only = 0;
       ca.real_io = p->c2r;
       ca.M = M;

@@ -61,6 +61,7 @@ struct ConvArgs {
                     // c2c + PNFFT_PRE_QUAD_PSI behaviour of the reference)
   int real_io;      // node arrays are real (c2r) instead of complex
   int accum;        // add into the node outputs (else store): ACCUMULATED, 2nd interlaced pass
+  int generic;      // use the one-thread-per-node kernels (set per plan, e.g. by an autotuner)
   int64_t M;
   const double *x;  // [M][3]
   void *grid;       // n0*n1*n2 complex in compute precision, natural order
