@@ -351,6 +351,7 @@ def run_gpu(args):
                             "ms_per_step": statistics.mean(ms_tab), "err_trafo_vs_ndft": err_tab}}
     if rank == 0 and world == 1 and not args.no_batch:
         line["batched"] = run_batched(P, torch, dev)
+        line["particles"] = run_particles(P, torch, dev)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in cpu_sample().items() if k != "seconds_per_step_extrapolated"}
     if rank == 0:
@@ -425,6 +426,60 @@ def run_batched(P, torch, dev, steps=5):
             "max_rel_err_fp32_vs_fp64_trafo": max(errs),
             "workload": "64 plans N_t in {16..128}, M log-uniform [1e3, 2^21], KB m 4..6, trafo+adj each; "
                         "8 RHS on one node set M=2^20 at N=64^3; one CUDA graph"}
+
+
+def run_particles(P, torch, dev, steps=3):
+    """Config 3: clustered real charges, c2r.  M = 2^21 (80% uniform, 20% from
+    64 Gaussian clusters of width 0.01, wrapped), weights +-1 with zero sum,
+    N = 64^3, n = 128^3, m = 5, Gaussian and B-spline windows, FP32-mixed.
+    A step is adj (charges to grid) + trafo with COMPUTE_F | COMPUTE_GRAD_F,
+    with the analytic (default) or the ik gradient (PNFFT_DIFF_IK).  Errors:
+    f_hat against the FP64 path, and the trafo against the FP64 NDFT on 4096
+    nodes for the same f_hat."""
+    from pnfft_gb300.particles import charges_c2r
+    rng = np.random.default_rng(3)
+    N, m, M = (64, 64, 64), 5, 2 ** 21
+    mc = M // 5
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    centres = rng.uniform(-0.5, 0.5, (64, 3))
+    x[:mc] = centres[rng.integers(0, 64, mc)] + 0.01 * rng.standard_normal((mc, 3))
+    x = np.mod(x + 0.5, 1.0) - 0.5
+    q = np.where(np.arange(M) % 2 == 0, 1.0, -1.0)
+    rng.shuffle(q)
+    xd, qd = torch.tensor(x, device=dev), torch.tensor(q, device=dev)
+    s = torch.cuda.current_stream(dev)
+    out = {}
+    for win, wflag in (("gaussian", P.WINDOW_GAUSSIAN), ("bspline", P.WINDOW_BSPLINE)):
+        for grad, gflag in (("analytic", 0), ("ik", P.DIFF_IK)):
+            p = P.Plan(N, m=m, flags=wflag | gflag, c2r=True, precision="fp32")
+            charges_c2r(p, xd, qd)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(s)
+            for _ in range(steps):
+                fh, phi, gphi = charges_c2r(p, xd, qd)
+            b.record(s)
+            b.synchronize()
+            ms = a.elapsed_time(b) / steps
+            ref = P.Plan(N, m=m, flags=wflag | gflag, c2r=True, precision="fp64")
+            fh64 = ref.adj_device(xd, qd)
+            sub = 4096
+            xs = xd[:sub].contiguous()
+            phid, gphid, _ = ref.trafo_device(xs, fh, P.COMPUTE_F | P.COMPUTE_GRAD_F | P.COMPUTE_DIRECT)
+            gphid = -gphid  # the reference's c2r NDFT returns minus the gradient (ndft-parallel.c:530-532)
+            phi64, gphi64, _ = ref.trafo_device(xs, fh, P.COMPUTE_F | P.COMPUTE_GRAD_F)
+            torch.cuda.synchronize()
+            rel = lambda u, v: (torch.linalg.vector_norm(u - v) / torch.linalg.vector_norm(v)).item()  # noqa: E731
+            out[f"{win}_{grad}"] = {"value": M / (ms * 1e-3) / 1e6, "unit": "Mpts/s", "ms_per_step": ms,
+                                    "err_f_hat_vs_fp64": rel(fh, fh64),
+                                    "err_phi_vs_fp64_ndft_4096": rel(phi[:sub], phid),
+                                    "err_grad_vs_fp64_ndft_4096": rel(gphi[:sub], gphid),
+                                    "window_aliasing_phi_fp64_nfft_vs_ndft": rel(phi64, phid),
+                                    "window_aliasing_grad_fp64_nfft_vs_ndft": rel(gphi64, gphid)}
+            p.close()
+            ref.close()
+    out["workload"] = ("c2r, N=64^3, n=128^3, M=2^21 (20% in 64 clusters, sigma 0.01), charges +-1, m=5; "
+                       "step = adj + trafo(F|GRAD_F), FP32-mixed")
+    return out
 
 
 def run_profile_case():

@@ -77,3 +77,56 @@ def test_grad_x_matches_compute_grad_f(lib, oracle):
     want = (np.conj(g.cpu().numpy())[:, None] * grad_f).real
     got = x.grad.cpu().numpy()
     assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-12
+
+
+def test_autograd_full_size_vs_fp64_central_differences(lib):
+    # the autograd workload: N=64^3, n=128^3, M=2^20, FP32-mixed plan, float32
+    # coordinates; FP64 central differences (h=1e-6) on 256 coordinates and
+    # 32 f_hat entries.  Differences are formed per node (the loss of 2^20
+    # terms would cancel): x_jt changes only f_j, and the loss is quadratic
+    # in f_hat with trafo(f_hat + h e_k) = f + h trafo(e_k).
+    torch = pytest.importorskip("torch")
+    if lib.device_count() == 0:
+        pytest.fail("no CUDA device")
+    from pnfft_gb300.autograd import trafo
+    rng = np.random.default_rng(23)
+    N, M, h = (64, 64, 64), 2 ** 20, 1e-6
+    S = 64 ** 3
+    plan = lib.Plan(N, m=6, precision="fp32")
+    ref = lib.Plan(N, m=6, precision="fp64")
+    x = torch.tensor(rng.uniform(-0.5, 0.5, (M, 3)), dtype=torch.float32, device="cuda", requires_grad=True)
+    fh = torch.tensor(rng.standard_normal(S) + 1j * rng.standard_normal(S), device="cuda", requires_grad=True)
+    y = torch.tensor(rng.standard_normal(M) + 1j * rng.standard_normal(M), device="cuda")
+    L = (torch.abs(trafo(fh, x, plan) - y) ** 2).sum()
+    L.backward()
+    x64 = x.detach().to(torch.float64)
+    fh64 = fh.detach()
+    with torch.no_grad():
+        f64, _, _ = ref.trafo_device(x64, fh64)
+        r = f64 - y
+        # coordinates
+        js = torch.tensor(rng.choice(M, 256, replace=False), device="cuda")
+        ts = torch.tensor(rng.integers(0, 3, 256), device="cuda")
+        xs = x64[js].clone()
+        xp, xm = xs.clone(), xs.clone()
+        xp[torch.arange(256), ts] += h
+        xm[torch.arange(256), ts] -= h
+        fpm, _, _ = ref.trafo_device(torch.cat([xp, xm]).contiguous(), fh64)
+        fd = (torch.abs(fpm[:256] - y[js]) ** 2 - torch.abs(fpm[256:] - y[js]) ** 2) / (2 * h)
+        ad = x.grad[js, ts].to(torch.float64)
+        err_x = (torch.linalg.vector_norm(ad - fd) / torch.linalg.vector_norm(fd)).item()
+        # f_hat entries
+        ks = rng.choice(S, 32, replace=False)
+        fd_fh, ad_fh = [], []
+        for k in ks:
+            e = torch.zeros(S, dtype=torch.complex128, device="cuda")
+            e[int(k)] = 1.0
+            gk, _, _ = ref.trafo_device(x64, e)
+            d_re = (torch.abs(r + h * gk) ** 2 - torch.abs(r - h * gk) ** 2).sum() / (2 * h)
+            d_im = (torch.abs(r + 1j * h * gk) ** 2 - torch.abs(r - 1j * h * gk) ** 2).sum() / (2 * h)
+            fd_fh.append(complex(d_re.item(), d_im.item()))
+            ad_fh.append(complex(fh.grad[int(k)].item()))
+        fd_fh, ad_fh = np.array(fd_fh), np.array(ad_fh)
+        err_f = np.linalg.norm(ad_fh - fd_fh) / np.linalg.norm(fd_fh)
+    assert err_x < 1e-6, err_x
+    assert err_f < 1e-6, err_f
