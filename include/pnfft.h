@@ -301,5 +301,6 @@ void pnfft_check_init_parameters(int argc, char **argv, ptrdiff_t *N, ptrdiff_t 
 #endif
 
 #include "pnfft_gb300.h"
+#include "pnfftf.h"
 
 #endif /* PNFFT_H */

@@ -20,7 +20,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["conv.cu", "deconv.cu", "sort.cu", "ndft.cu", "engine.cu"]
-CPP_SOURCES = ["api.cpp"]
+CPP_SOURCES = ["api.cpp", "api_float.cpp"]
 
 
 def _deps():
@@ -58,7 +58,7 @@ def build(force=False, verbose=False, jobs=None):
                      os.path.join(CSRC, s), "-o", o])
     for s in CPP_SOURCES:
         o = os.path.join(OBJ, s + ".o")
-        cmds.append(["g++", "-fPIC", "-Wall", "-Wno-unused-function", *common, "-I",
+        cmds.append(["g++", "-fPIC", "-Wall", "-Wno-unused-function", "-ffp-contract=off", *common, "-I",
                      os.path.join(CUDA_HOME, "include"), "-c", os.path.join(CSRC, s), "-o", o])
     jobs = jobs or min(len(cmds), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(jobs) as ex:

@@ -151,3 +151,68 @@ def test_no_gpu_fails_loudly(lib):
     x = np.zeros((4, 3))
     with pytest.raises(lib.PnfftError, match="no CUDA device"):
         p.trafo(x, np.zeros(512, complex))
+
+
+def test_float_api_exports_and_generators(lib):
+    # the single-precision instantiation pnfftf_* (api/pnfft.h:287)
+    L = lib.load()
+    src = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "pnfftf.h")).read(), flags=re.S)
+    names = set(re.findall(r"\b(pnfftf_[A-Za-z0-9_]+)\s*\(", src))
+    assert len(names) > 80
+    assert not [n for n in sorted(names) if not hasattr(L, n)]
+    # pnfftf_init_x_3d with R = float (api-adv.c:35-86): (float)rand()/RAND_MAX below 1,
+    # then (up - lo) * t + lo in float, against the same expressions in numpy float32
+    libc = ctypes.CDLL(None)
+    f3 = ctypes.c_float * 3
+    lo, up = f3(-0.5, -0.25, -0.5), f3(0.5, 0.25, 0.125)
+    x = (ctypes.c_float * 60)()
+    fn = L.pnfftf_init_x_3d
+    fn.argtypes = [ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float), ctypes.c_ssize_t,
+                   ctypes.POINTER(ctypes.c_float)]
+    fn.restype = None
+    libc.srand(7)
+    fn(lo, up, 20, x)
+    libc.srand(7)
+    want = []
+    for _ in range(20):
+        for t in range(3):
+            while True:
+                while True:
+                    v = np.float32(libc.rand()) / np.float32(2147483647)
+                    if v < np.float32(1.0):
+                        break
+                v = (np.float32(up[t]) - np.float32(lo[t])) * v + np.float32(lo[t])
+                if not (v < -np.float32(0.5) or np.float32(0.5) <= v):
+                    break
+            want.append(v)
+    np.testing.assert_array_equal(np.array(list(x), dtype=np.float32), np.array(want, dtype=np.float32))
+    # pnfftf_init_f: 100.0 * (float)rand() / RAND_MAX in double, rounded to float
+    f = (ctypes.c_float * 20)()
+    L.pnfftf_init_f.argtypes = [ctypes.c_ssize_t, ctypes.c_void_p]
+    L.pnfftf_init_f.restype = None
+    libc.srand(8)
+    L.pnfftf_init_f(10, f)
+    libc.srand(8)
+    want = [np.float32(100.0 * float(np.float32(libc.rand())) / 2147483647) for _ in range(20)]
+    np.testing.assert_array_equal(np.array(list(f), dtype=np.float32), np.array(want, dtype=np.float32))
+    # plan getters and window values agree with the double plan
+    N = (ctypes.c_ssize_t * 3)(8, 10, 12)
+    n = (ctypes.c_ssize_t * 3)(16, 20, 24)
+    L.pnfftf_init_guru.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                   ctypes.c_uint, ctypes.c_uint, ctypes.c_int]
+    L.pnfftf_init_guru.restype = ctypes.c_void_p
+    p = L.pnfftf_init_guru(3, N, n, f3(0.5, 0.5, 0.5), 4, lib.MALLOC_F_HAT, lib.PFFT_ESTIMATE, lib.MPI_COMM_WORLD)
+    assert p
+    for name in ("pnfftf_get_m", "pnfftf_get_d"):
+        getattr(L, name).argtypes = [ctypes.c_void_p]
+    assert L.pnfftf_get_m(p) == 4 and L.pnfftf_get_d(p) == 3
+    L.pnfftf_gb300_double_plan.argtypes = [ctypes.c_void_p]
+    L.pnfftf_gb300_double_plan.restype = ctypes.c_void_p
+    dp = L.pnfftf_gb300_double_plan(p)
+    assert L.pnfft_gb300_get_precision(dp) == lib.GB300_FP32_MIXED
+    L.pnfftf_psi.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_float]
+    L.pnfftf_psi.restype = ctypes.c_float
+    for xv in (0.0, 0.03, -0.07):
+        assert L.pnfftf_psi(p, 1, xv) == np.float32(L.pnfft_psi(dp, 1, float(np.float32(xv))))
+    L.pnfftf_finalize.argtypes = [ctypes.c_void_p, ctypes.c_uint]
+    L.pnfftf_finalize(p, lib.FREE_F_HAT)
