@@ -46,6 +46,17 @@ def make_inputs(seed=2):
     return x, fh, f
 
 
+def replica_throughput(local_seconds, units_per_rank, world, dist=None, device=None):
+    """Whole-job throughput of N independent replicas: every rank processes
+    units_per_rank units; the job time is the slowest rank's (MAX all-reduce),
+    so value = world * units_per_rank / max_rank_seconds."""
+    import torch
+    t = torch.tensor([float(local_seconds)], dtype=torch.float64, device=device)
+    if dist is not None and world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return world * units_per_rank / t.item(), t.item()
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -223,10 +234,8 @@ def run_gpu(args):
     ms, stage_b, f32_out, fh32_out = device_steps(p32, args.steps, args.warmup)
     clocks = sampler.stop()
     step_ms = sum(ms) / len(ms)
-    t_max = torch.tensor([sum(ms)], device=dev)
-    if dist is not None:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    value = world * M * args.steps / (t_max.item() * 1e-3) / 1e6
+    value, _ = replica_throughput(sum(ms) * 1e-3, M * args.steps, world, dist, dev)
+    value /= 1e6
 
     # amortised: nodes declared fixed (binning reused)
     p32f = P.Plan(N, n, m=m, precision="fp32")
@@ -317,10 +326,8 @@ def run_gpu(args):
         t3 = time.perf_counter()
         e2e_s.append((t1 - t0) + (t3 - t2))
     barrier()
-    tsum = torch.tensor([sum(e2e_s)], device=dev)
-    if dist is not None:
-        dist.all_reduce(tsum, op=dist.ReduceOp.MAX)
-    e2e_value = world * M * args.steps / tsum.item() / 1e6
+    e2e_value, _ = replica_throughput(sum(e2e_s), M * args.steps, world, dist, dev)
+    e2e_value /= 1e6
     nfh = int(np.prod(N))
     h2d = 2 * M * 24 + nfh * 16 + M * 16
     d2h = M * 16 + nfh * 16
