@@ -475,6 +475,7 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
     __syncthreads();
     // node-fastest: a warp shares one (axis, stencil point), so the fitted
     // polynomial rows are broadcast loads
+#pragma unroll 2  // two independent polynomial chains per thread
     for (int v = tid; v < NBI * 3 * CUT; v += blockDim.x) {
       const int e = v / NBI, i = v - e * NBI;
       if (i >= nb) continue;
@@ -950,6 +951,7 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
     // --- window values: all threads over (node, axis, stencil point) ------------
     // node-fastest (broadcast polynomial rows); the odd row stride in 16-byte
     // units keeps these stores to at most 4-way bank conflicts
+#pragma unroll 2  // two independent polynomial chains per thread
     for (int v = tid; v < NB * 3 * CUT; v += nth) {
       const int e = v / NB, i = v - e * NB;
       if (i >= nb) continue;
@@ -970,6 +972,7 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
         for (int z = 0; z < W; z++) acc_r[c][z] = acc_i[c][z] = (T)0;
       since = 0;
     }
+#pragma unroll 2
     for (int i = 0; i < nb; i++) {
       const int pk = s_o[i];
       const int slab = (pk >> 16) / TL;
