@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <stdio.h>
 
+#include <atomic>
+
 #include "pg_index.cuh"
 #include "pg_kernels.h"
 #include "pg_math.cuh"
@@ -1088,10 +1090,14 @@ void choose_tiles(int cut, bool fp32, bool spread, const int *n, int *T, int *li
 template <typename T, int CUT, int MODE>
 static void run_interp_tile(const ConvArgs &a, cudaStream_t s) {
   const size_t sm = InterpGeom<T, CUT, MODE>::SMEM;
-  static bool attr_done = false;
-  if (!attr_done) {
+  // the shared-memory opt-in is a per-device attribute of the kernel
+  static std::atomic<unsigned long long> attr_done{0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(attr_done.load() & bit)) {
     cudaFuncSetAttribute(k_interp_tile<T, CUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    attr_done = true;
+    attr_done.fetch_or(bit);
   }
   k_interp_tile<T, CUT, MODE><<<a.bin.max_subs, kThreads, sm, s>>>(a);
 }

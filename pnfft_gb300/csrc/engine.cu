@@ -53,6 +53,9 @@ struct Stage {
 struct DevState {
   int device = -1;
   cudaStream_t own = nullptr, stream = nullptr;
+  // the trafo bins its nodes on `aux` while D and the FFT run on `stream`
+  cudaStream_t aux = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   void *grid = nullptr;
   size_t grid_bytes = 0;
   cufftHandle fft = 0;
@@ -136,6 +139,9 @@ static int ensure_dev(pnfft_plan p) {
     }
     PG_CUDA(cudaGetDevice(&d->device));
     PG_CUDA(cudaStreamCreateWithFlags(&d->own, cudaStreamNonBlocking));
+    PG_CUDA(cudaStreamCreateWithFlags(&d->aux, cudaStreamNonBlocking));
+    PG_CUDA(cudaEventCreateWithFlags(&d->ev_fork, cudaEventDisableTiming));
+    PG_CUDA(cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming));
   }
   d->stream = p->user_stream ? (cudaStream_t)p->user_stream : d->own;
   return 0;
@@ -378,17 +384,18 @@ static cudaEvent_t get_event(DevState *d) {
 struct StageScope {
   DevState *d;
   Stage st;
-  StageScope(DevState *d_, int idx, int adj) : d(d_) {
+  cudaStream_t s;
+  StageScope(DevState *d_, int idx, int adj, cudaStream_t s_ = nullptr) : d(d_), s(s_ ? s_ : d_->stream) {
     if (d->capturing) return;  // no stage timers inside a captured graph
     st.idx = idx;
     st.adj = adj;
     st.a = get_event(d);
     st.b = get_event(d);
-    cudaEventRecord(st.a, d->stream);
+    cudaEventRecord(st.a, s);
   }
   ~StageScope() {
     if (d->capturing) return;
-    cudaEventRecord(st.b, d->stream);
+    cudaEventRecord(st.b, s);
     d->pending.push_back(st);
   }
 };
@@ -474,15 +481,16 @@ static int fft_exec(pnfft_plan p, int direction) {
 }
 
 // bins the nodes for pass `il` unless a valid binning of the same fixed nodes exists
-static int do_binning(pnfft_plan p, pnfft_nodes nd, ConvArgs &a, int il, int adj) {
+static int do_binning(pnfft_plan p, pnfft_nodes nd, ConvArgs &a, int il, int adj, cudaStream_t s = nullptr) {
   DevState *d = p->dev;
+  if (!s) s = d->stream;
   if (ensure_binning(p, nd->local_M, adj, il)) return -1;
   DevState::BinSlot &sl = d->bins[adj][il];
   a.bin = sl.b;
   bool reuse = nd->fixed && sl.valid && sl.uid == nd->uid && sl.ver == nd->version;
   if (!reuse) {
-    StageScope sc(d, PNFFT_TIMER_SORT_NODES, adj);
-    bin_nodes(a, fp32(p), d->stream);
+    StageScope sc(d, PNFFT_TIMER_SORT_NODES, adj, s);
+    bin_nodes(a, fp32(p), s);
     sl.valid = true;
     sl.uid = nd->uid;
     sl.ver = nd->version;
@@ -496,8 +504,10 @@ struct Arrays {
   double *fhat;             // f_hat on the device
 };
 
-static int resolve_arrays(pnfft_plan p, pnfft_nodes nd, unsigned cflags, bool adjoint, Arrays &A, bool &zero_copy) {
+static int resolve_arrays(pnfft_plan p, pnfft_nodes nd, unsigned cflags, bool adjoint, Arrays &A, bool &zero_copy,
+                          cudaStream_t xs = nullptr) {
   DevState *d = p->dev;
+  if (!xs) xs = d->stream;
   int64_t M = nd ? nd->local_M : 0;
   const int tuple = p->c2r ? 1 : 2;
   zero_copy = nd && nd->u_x;
@@ -526,7 +536,7 @@ static int resolve_arrays(pnfft_plan p, pnfft_nodes nd, unsigned cflags, bool ad
           if ((cflags & C_HESS) && !nd->hessian_f)
             return set_error("pnfft_trafo: missing memory allocation of nodes->hessian_f"), -1;
         }
-        PG_CUDA(cudaMemcpyAsync(v->x, nd->x, sizeof(double) * 3 * M, cudaMemcpyHostToDevice, d->stream));
+        PG_CUDA(cudaMemcpyAsync(v->x, nd->x, sizeof(double) * 3 * M, cudaMemcpyHostToDevice, xs));
         bool upload_out = !adjoint && (cflags & PNFFT_COMPUTE_ACCUMULATED);
         if ((cflags & C_F) && (adjoint || upload_out)) {
           if (!nd->f) {
@@ -614,9 +624,17 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
   const int tuple = p->c2r ? 1 : 2;
   Arrays A;
   bool zc = false;
+  // the node work (copy of x, binning) runs on the auxiliary stream, forked
+  // from the plan's stream, while D and F run; B waits for it
+  const bool fork = nd && M > 0 && !(cflags & (PNFFT_OMIT_CONV | PNFFT_COMPUTE_DIRECT));
+  cudaStream_t xs = fork ? d->aux : s;
+  if (fork) {
+    PG_CUDA(cudaEventRecord(d->ev_fork, s));
+    PG_CUDA(cudaStreamWaitEvent(d->aux, d->ev_fork, 0));
+  }
   {
     StageScope whole(d, PNFFT_TIMER_WHOLE, 0);
-    if (resolve_arrays(p, nd, cflags, false, A, zc)) return -1;
+    if (resolve_arrays(p, nd, cflags, false, A, zc, xs)) return -1;
     // zero the outputs (api-basic.c:210-222; trafo_A always overwrites, 400-414)
     bool zero = (!(cflags & PNFFT_COMPUTE_ACCUMULATED) && !(cflags & PNFFT_OMIT_CONV)) ||
                 (cflags & PNFFT_COMPUTE_DIRECT);
@@ -631,6 +649,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
     if ((cflags & C_HESS) && M > 0 && !A.hess)
       return set_error("pnfft_trafo: missing memory allocation of nodes->hessian_f"), -1;
 
+    bool joined = !fork;
     if (cflags & PNFFT_COMPUTE_DIRECT) {
       NdftArgs na;
       memset(&na, 0, sizeof(na));
@@ -664,13 +683,23 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       ca.grid = d->grid;
       DeconvArgs da = deconv_args(p);
       da.fhat_in = A.fhat;
+      Binning pass_bin[2] = {};
+      if (fork) {
+        for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
+          ca.il = il_plan ? pass : 0;
+          if (do_binning(p, nd, ca, ca.il, 0, d->aux)) return -1;
+          pass_bin[pass] = ca.bin;
+        }
+        PG_CUDA(cudaEventRecord(d->ev_join, d->aux));
+      }
+      joined = !fork;
       for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
         const int il = il_plan ? pass : 0;
         ca.use_il = il_plan ? 1 : 0;
         ca.il = il;
         ca.accum = (pass > 0 || (cflags & PNFFT_COMPUTE_ACCUMULATED)) ? 1 : 0;
         da.interlaced = il;
-        if (nd && !(cflags & PNFFT_OMIT_CONV) && do_binning(p, nd, ca, il, 0)) return -1;
+        ca.bin = pass_bin[pass];
         auto one = [&](int ikmode, int ikdim, double *out, int64_t off, int64_t stride, int mode) -> int {
           {
             StageScope sc(d, PNFFT_TIMER_MATRIX_D, 0);
@@ -683,6 +712,10 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
             if (!(cflags & PNFFT_OMIT_FFT) && fft_exec(p, CUFFT_FORWARD)) return -1;
           }
           if (!(cflags & PNFFT_OMIT_CONV) && nd) {
+            if (!joined) {  // B needs the binning from the auxiliary stream
+              PG_CUDA(cudaStreamWaitEvent(s, d->ev_join, 0));
+              joined = true;
+            }
             StageScope sc(d, PNFFT_TIMER_MATRIX_B, 0);
             ConvArgs c = ca;
             c.offset = off;
@@ -716,6 +749,10 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
             if (!(cflags & PNFFT_OMIT_FFT) && fft_exec(p, CUFFT_FORWARD)) return -1;
           }
           if (!(cflags & PNFFT_OMIT_CONV) && nd) {
+            if (!joined) {
+              PG_CUDA(cudaStreamWaitEvent(s, d->ev_join, 0));
+              joined = true;
+            }
             StageScope sc(d, PNFFT_TIMER_MATRIX_B, 0);
             ConvArgs c = ca;
             c.offset = 0;
@@ -730,6 +767,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
         }
       }
     }
+    if (!joined) PG_CUDA(cudaStreamWaitEvent(s, d->ev_join, 0));  // every path joins the fork
     if (!zc && M > 0) {
       if (cflags & C_F) PG_CUDA(cudaMemcpyAsync(nd->f, A.f, sizeof(double) * tuple * M, cudaMemcpyDeviceToHost, s));
       if (cflags & C_GRAD)
@@ -896,6 +934,9 @@ void engine_release_plan(pnfft_plan p) {
       for (auto &sl : row) free_binning(sl.b);
     for (cudaEvent_t e : d->free_ev) cudaEventDestroy(e);
     if (d->own) cudaStreamDestroy(d->own);
+    if (d->aux) cudaStreamDestroy(d->aux);
+    if (d->ev_fork) cudaEventDestroy(d->ev_fork);
+    if (d->ev_join) cudaEventDestroy(d->ev_join);
     cudaGetLastError();
   }
   delete d;
