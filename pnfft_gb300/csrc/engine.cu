@@ -798,9 +798,17 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
   Arrays A;
   bool zc = false;
   size_t fb = sizeof(double) * 2 * (size_t)p->local_N_total;
+  // as in the trafo: the copy of x and the binning run on the auxiliary
+  // stream while the plan's stream uploads f and clears f_hat and the grid
+  const bool fork = nd && M > 0 && !(cflags & (PNFFT_OMIT_CONV | PNFFT_COMPUTE_DIRECT));
+  if (fork) {
+    PG_CUDA(cudaEventRecord(d->ev_fork, s));
+    PG_CUDA(cudaStreamWaitEvent(d->aux, d->ev_fork, 0));
+  }
+  bool joined = !fork;
   {
     StageScope whole(d, PNFFT_TIMER_WHOLE, 1);
-    if (resolve_arrays(p, nd, cflags, true, A, zc)) return -1;
+    if (resolve_arrays(p, nd, cflags, true, A, zc, fork ? d->aux : s)) return -1;
     if (!(cflags & PNFFT_COMPUTE_ACCUMULATED) && fb > 0) PG_CUDA(cudaMemsetAsync(A.fhat, 0, fb, s));
     if ((cflags & C_F) && M > 0 && !A.f) return set_error("pnfft_adj: missing memory allocation of nodes->f"), -1;
     if ((cflags & C_GRAD) && M > 0 && !A.grad)
@@ -839,17 +847,30 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       ca.grid = d->grid;
       DeconvArgs da = deconv_args(p);
       da.fhat_out = A.fhat;
+      Binning pass_bin[2] = {};
+      if (fork) {
+        for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
+          ca.il = il_plan ? pass : 0;
+          if (do_binning(p, nd, ca, ca.il, 1, d->aux)) return -1;
+          pass_bin[pass] = ca.bin;
+        }
+        PG_CUDA(cudaEventRecord(d->ev_join, d->aux));
+      }
       for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
         const int il = il_plan ? pass : 0;
         ca.use_il = il_plan ? 1 : 0;
         ca.il = il;
         da.interlaced = il;
-        if (nd && !(cflags & PNFFT_OMIT_CONV) && do_binning(p, nd, ca, il, 1)) return -1;
+        ca.bin = pass_bin[pass];
         auto one = [&](int ikmode, int ikdim, const double *fin, const double *gin, int64_t off, int64_t stride,
                        int mode) -> int {
+          PG_CUDA(cudaMemsetAsync(d->grid, 0, gbytes, s));
+          if (!joined) {  // B^T needs the binning from the auxiliary stream
+            PG_CUDA(cudaStreamWaitEvent(s, d->ev_join, 0));
+            joined = true;
+          }
           {
             StageScope sc(d, PNFFT_TIMER_MATRIX_B, 1);
-            PG_CUDA(cudaMemsetAsync(d->grid, 0, gbytes, s));
             if (!(cflags & PNFFT_OMIT_CONV) && nd) {
               ConvArgs c = ca;
               c.offset = off;
@@ -882,6 +903,7 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
         }
       }
     }
+    if (!joined) PG_CUDA(cudaStreamWaitEvent(s, d->ev_join, 0));  // every path joins the fork
     if (!p->d_f_hat_user && fb > 0) {
       if (!p->f_hat) return set_error("pnfft_adj: f_hat is not allocated"), -1;
       PG_CUDA(cudaMemcpyAsync(p->f_hat, A.fhat, fb, cudaMemcpyDeviceToHost, s));
