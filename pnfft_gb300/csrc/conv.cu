@@ -75,8 +75,9 @@ __device__ __forceinline__ AxisPos axis_pos(double x, int n, int m, int il) {
 //
 // k_bin_keys computes, once per node, the lowest stencil index u (bit-exact)
 // and the fractional positions, writes the node record (unsorted) and counts
-// nodes per tile; a three-phase scan gives tile starts and the sub-problem
-// list; k_bin_scatter moves perm and records into tile order.
+// nodes per tile (the count before its own increment is the node's rank in
+// the tile); a three-phase scan gives tile starts and the sub-problem list;
+// k_bin_scatter moves perm and records to start[tile] + rank.
 // For the FP32-mixed form without interlacing, floor(fl(n x)) is evaluated
 // with integer arithmetic on the bits of x (the FP64 pipe of GB300 is slow):
 // the exact product n*M_x (<= 73 bits) is rounded to 53 bits with ties to
@@ -118,7 +119,7 @@ __global__ void k_bin_keys(const double *__restrict__ x, int64_t M, int n0, int 
   const int opk = (u[0] - t0 * b.T[0]) | ((u[1] - t1 * b.T[1]) << 8) | (z << 16);
   b.key[j] = tile;
   store_rec(rec_unsorted, j, dist, opk, T(0));
-  atomicAdd(&b.count[tile], 1);
+  b.rank[j] = atomicAdd(&b.count[tile], 1);  // position of the node within its tile
 }
 
 // three-phase exclusive scan of the tile counts and sub-problem counts
@@ -223,7 +224,6 @@ __global__ void __launch_bounds__(256) k_bin_scan_c(Binning b, const int *bsum) 
     const int i = k0 + k;
     if (i < n) {
       b.start[lo + i] = oa;
-      b.cursor[lo + i] = 0;
       b.nsub_tile[lo + i] = cb[i];
       b.sub_off[lo + i] = ob;
     }
@@ -236,8 +236,7 @@ template <typename T>
 __global__ void k_bin_scatter(int64_t M, Binning b, const void *__restrict__ rec_unsorted) {
   int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= M) return;
-  const int t = b.key[j];
-  const int pos = b.start[t] + atomicAdd(&b.cursor[t], 1);
+  const int pos = b.start[b.key[j]] + b.rank[j];
   b.perm[pos] = (int)j;
   if (sizeof(T) == 4) ((float4 *)b.rec)[pos] = ((const float4 *)rec_unsorted)[j];
   else ((double4 *)b.rec)[pos] = ((const double4 *)rec_unsorted)[j];

@@ -20,6 +20,8 @@
 // element is float2 or double2.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pg_kernels.h"
 
 namespace pg {
@@ -114,64 +116,60 @@ __global__ void k_deconv_pad(DeconvArgs a) {
   }
 }
 
+// One CTA per row of the stored f_hat block (grid-stride), threads along its
+// fastest axis (k2, or k0 for TRANSPOSED_F_HAT): f_hat[k] += D grid[k mod n].
 template <typename C>
 __global__ void k_deconv_crop_acc(DeconvArgs a) {
-  const int64_t total = a.Nl[0] * a.Nl[1] * a.Nl[2];
   const C *grid = (const C *)a.grid;
   double2 *fh = (double2 *)a.fhat_out;
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    int64_t a0, a1, a2;
-    if (a.transposed) {
-      a0 = idx % a.Nl[0];
-      int64_t r = idx / a.Nl[0];
-      a2 = r % a.Nl[2];
-      a1 = r / a.Nl[2];
-    } else {
-      a2 = idx % a.Nl[2];
-      int64_t r = idx / a.Nl[2];
-      a1 = r % a.Nl[1];
-      a0 = r / a.Nl[1];
+  // storage axes, outer to inner
+  const int o0 = a.transposed ? 1 : 0, o1 = a.transposed ? 2 : 1, o2 = a.transposed ? 0 : 2;
+  const int64_t rows = a.Nl[o0] * a.Nl[o1], len = a.Nl[o2];
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int64_t ra = r / a.Nl[o1], rb = r - ra * a.Nl[o1];
+    for (int64_t c = threadIdx.x; c < len; c += blockDim.x) {
+      int64_t ax[3];
+      ax[o0] = ra;
+      ax[o1] = rb;
+      ax[o2] = c;
+      const long long k[3] = {a.ks[0] + ax[0], a.ks[1] + ax[1], a.ks[2] + ax[2]};
+      int64_t g[3];  // k mod n; |k| <= N/2 <= n/2
+      for (int t = 0; t < 3; t++) g[t] = k[t] < 0 ? k[t] + a.n[t] : k[t];
+      double2 v = to_d(grid[(g[0] * a.n[1] + g[1]) * a.n[2] + g[2]]);
+      if (a.ik) v = cmul(v, ik_factor(a, k, true));
+      if (a.interlaced) {
+        double h = ((double)k[0] / (double)a.n[0] + (double)k[1] / (double)a.n[1]) + (double)k[2] / (double)a.n[2];
+        double sn, cs;
+        sincospi(h, &sn, &cs);
+        v = cmul(v, make_double2(cs, -sn));
+      }
+      const double w = (a.inv[0][ax[0]] * a.inv[1][ax[1]]) * a.inv[2][ax[2]] * a.scale;
+      const int64_t idx = r * len + c;
+      double2 o = fh[idx];
+      o.x += v.x * w;
+      o.y += v.y * w;
+      fh[idx] = o;
     }
-    long long k[3] = {a.ks[0] + a0, a.ks[1] + a1, a.ks[2] + a2};
-    int64_t g[3];
-    for (int t = 0; t < 3; t++) {
-      long long kk = k[t] % a.n[t];
-      g[t] = kk < 0 ? kk + a.n[t] : kk;
-    }
-    double2 v = to_d(grid[(g[0] * a.n[1] + g[1]) * a.n[2] + g[2]]);
-    if (a.ik) v = cmul(v, ik_factor(a, k, true));
-    if (a.interlaced) {
-      double h = ((double)k[0] / (double)a.n[0] + (double)k[1] / (double)a.n[1]) + (double)k[2] / (double)a.n[2];
-      double sn, cs;
-      sincospi(h, &sn, &cs);
-      v = cmul(v, make_double2(cs, -sn));
-    }
-    double w = (a.inv[0][a0] * a.inv[1][a1]) * a.inv[2][a2] * a.scale;
-    double2 o = fh[idx];
-    o.x += v.x * w;
-    o.y += v.y * w;
-    fh[idx] = o;
   }
 }
 
-static unsigned blocks_for(int64_t total, int th) {
-  int64_t b = (total + th - 1) / th;
-  if (b > 152 * 64) b = 152 * 64;
-  if (b < 1) b = 1;
-  return (unsigned)b;
-}
+static int row_threads(int64_t len) { return len >= 256 ? 256 : (len >= 128 ? 128 : 64); }
 
 void launch_deconv_pad(const DeconvArgs &a, bool fp32, cudaStream_t s) {
-  int64_t total = (int64_t)a.n[0] * a.n[1] * a.n[2];
-  if (fp32) k_deconv_pad<float2><<<blocks_for(total, 256), 256, 0, s>>>(a);
-  else k_deconv_pad<double2><<<blocks_for(total, 256), 256, 0, s>>>(a);
+  const int64_t total = (int64_t)a.n[0] * a.n[1] * a.n[2];
+  const unsigned bl = (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152 * 64));
+  if (fp32) k_deconv_pad<float2><<<bl, 256, 0, s>>>(a);
+  else k_deconv_pad<double2><<<bl, 256, 0, s>>>(a);
 }
 
 void launch_deconv_crop_acc(const DeconvArgs &a, bool fp32, cudaStream_t s) {
-  int64_t total = a.Nl[0] * a.Nl[1] * a.Nl[2];
-  if (fp32) k_deconv_crop_acc<float2><<<blocks_for(total, 256), 256, 0, s>>>(a);
-  else k_deconv_crop_acc<double2><<<blocks_for(total, 256), 256, 0, s>>>(a);
+  const int o1 = a.transposed ? 2 : 1, o2 = a.transposed ? 0 : 2, o0 = a.transposed ? 1 : 0;
+  const int64_t rows = a.Nl[o0] * a.Nl[o1];
+  if (rows <= 0 || a.Nl[o2] <= 0) return;
+  const int th = row_threads(a.Nl[o2]);
+  const unsigned bl = (unsigned)std::min<int64_t>(rows, 152 * 64);
+  if (fp32) k_deconv_crop_acc<float2><<<bl, th, 0, s>>>(a);
+  else k_deconv_crop_acc<double2><<<bl, th, 0, s>>>(a);
 }
 
 }  // namespace pg

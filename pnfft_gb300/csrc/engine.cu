@@ -289,7 +289,7 @@ static int ensure_tables(pnfft_plan p) {
 }
 
 static void free_binning(Binning &b) {
-  int **arrs[] = {&b.key, &b.perm, &b.count, &b.start, &b.cursor, &b.nsub_tile, &b.sub_off, &b.sub_tile,
+  int **arrs[] = {&b.key, &b.perm, &b.count, &b.start, &b.rank, &b.nsub_tile, &b.sub_off, &b.sub_tile,
                   &b.sub_first, &b.sub_cnt, &b.nsub};
   for (int **a : arrs) {
     if (*a) cudaFree(*a);
@@ -326,7 +326,7 @@ static int ensure_binning(pnfft_plan p, int64_t M, int spread, int il) {
   PG_CUDA(cudaMalloc(&b.perm, sizeof(int) * cap));
   PG_CUDA(cudaMalloc(&b.count, sizeof(int) * b.ntiles));
   PG_CUDA(cudaMalloc(&b.start, sizeof(int) * b.ntiles));
-  PG_CUDA(cudaMalloc(&b.cursor, sizeof(int) * b.ntiles));
+  PG_CUDA(cudaMalloc(&b.rank, sizeof(int) * cap));
   PG_CUDA(cudaMalloc(&b.nsub_tile, sizeof(int) * b.ntiles));
   PG_CUDA(cudaMalloc(&b.sub_off, sizeof(int) * b.ntiles));
   PG_CUDA(cudaMalloc(&b.sub_tile, sizeof(int) * b.max_subs));

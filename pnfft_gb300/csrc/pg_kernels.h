@@ -40,7 +40,7 @@ struct Binning {
   int *perm;       // [M] nodes sorted by tile
   int *count;      // [ntiles]
   int *start;      // [ntiles]
-  int *cursor;     // [ntiles]
+  int *rank;       // [M] position of each node within its tile
   int *nsub_tile;  // [ntiles]
   int *sub_off;    // [ntiles]
   int *sub_tile;   // [max_subs]
