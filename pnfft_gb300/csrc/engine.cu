@@ -85,6 +85,9 @@ struct DevState {
 struct NodeDev {
   double *x = nullptr, *f = nullptr, *grad = nullptr, *hess = nullptr;
   int64_t cap = 0;
+  // the device copy of x matches the host x of this version (fixed nodes only)
+  bool x_valid = false;
+  uint64_t x_ver = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -355,6 +358,7 @@ static int ensure_node_buffers(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
     cudaFree(v->hess);
     v->x = v->f = v->grad = v->hess = nullptr;
     v->cap = 0;
+    v->x_valid = false;
     size_t m = (size_t)std::max<int64_t>(M, 1);
     PG_CUDA(cudaMalloc(&v->x, sizeof(double) * 3 * m));
     PG_CUDA(cudaMalloc(&v->f, sizeof(double) * 2 * m));
@@ -536,7 +540,13 @@ static int resolve_arrays(pnfft_plan p, pnfft_nodes nd, unsigned cflags, bool ad
           if ((cflags & C_HESS) && !nd->hessian_f)
             return set_error("pnfft_trafo: missing memory allocation of nodes->hessian_f"), -1;
         }
-        PG_CUDA(cudaMemcpyAsync(v->x, nd->x, sizeof(double) * 3 * M, cudaMemcpyHostToDevice, xs));
+        // fixed nodes (pnfft_precompute_psi / pnfft_gb300_nodes_set_fixed): the
+        // coordinates are promised constant, so the device copy is reused
+        if (!(nd->fixed && v->x_valid && v->x_ver == nd->version)) {
+          PG_CUDA(cudaMemcpyAsync(v->x, nd->x, sizeof(double) * 3 * M, cudaMemcpyHostToDevice, xs));
+          v->x_valid = true;
+          v->x_ver = nd->version;
+        }
         bool upload_out = !adjoint && (cflags & PNFFT_COMPUTE_ACCUMULATED);
         if ((cflags & C_F) && (adjoint || upload_out)) {
           if (!nd->f) {

@@ -299,3 +299,25 @@ def test_zero_copy_device_api_matches_host(gpu):
     assert rel(fd.cpu().numpy(), fa) < 1e-6
     assert rel(gd.cpu().numpy(), ga) < 1e-6
     assert rel(ad.cpu().numpy(), aa) < 1e-6
+
+
+def test_fixed_nodes_reuse_device_coordinates(gpu, oracle):
+    # with fixed nodes the device copy of x and the binning are reused across
+    # host-array calls; a new x array (pnfft_set_x with another pointer) or
+    # releasing the promise brings the new coordinates in
+    N = (16, 16, 16)
+    x, fh, f, g = case(N, 800, 17)
+    L = gpu.load()
+    p = gpu.Plan(N, m=5, precision="fp32")
+    o = oracle.OraclePlan(N, m=5)
+    nd = p._nodes_for(x.shape[0])
+    L.pnfft_gb300_nodes_set_fixed(nd, 1)
+    a1 = p.trafo(x, fh)[0].copy()
+    a2 = p.trafo(x, fh)[0].copy()
+    np.testing.assert_array_equal(a1, a2)
+    assert rel(a1, o.trafo(x, fh)[0]) < 3e-6
+    x2 = np.ascontiguousarray(np.roll(x, 1, axis=0))  # another array: pnfft_set_x sees a new pointer
+    b = p.trafo(x2, fh)[0]
+    assert rel(b, o.trafo(x2, fh)[0]) < 3e-6
+    L.pnfft_gb300_nodes_set_fixed(nd, 0)
+    assert rel(p.adj(x, f), o.adj(x, f)) < 3e-6
