@@ -321,3 +321,19 @@ def test_fixed_nodes_reuse_device_coordinates(gpu, oracle):
     assert rel(b, o.trafo(x2, fh)[0]) < 3e-6
     L.pnfft_gb300_nodes_set_fixed(nd, 0)
     assert rel(p.adj(x, f), o.adj(x, f)) < 3e-6
+
+
+@pytest.mark.parametrize("flags", ["interlaced", "diff_ik", "interlaced_ik", "transposed_interlaced"])
+def test_c2r_mode_combinations(gpu, oracle, flags):
+    fl = {"interlaced": gpu.INTERLACED, "diff_ik": gpu.DIFF_IK, "interlaced_ik": gpu.INTERLACED | gpu.DIFF_IK,
+          "transposed_interlaced": gpu.TRANSPOSED_F_HAT | gpu.INTERLACED}[flags]
+    N = (12, 8, 16)
+    for prec, tol in (("fp64", FP64_TOL), ("fp32", 3e-6)):
+        p = gpu.Plan(N, m=4, flags=fl, c2r=True, precision=prec)
+        o = oracle.OraclePlan(N, m=4, flags=fl, c2r=True)
+        x, fh, f, g = case(N, 600, 18, c2r=True, local_N=p.local_N)
+        a = p.trafo(x, fh, CF_ALL)
+        b = o.trafo(x, fh, CF_ALL)
+        for u, v in zip(a, b):
+            assert rel(u, v) < tol, (flags, prec)
+        assert rel(p.adj(x, f, g, 1 | 2), o.adj(x, f, g, 1 | 2)) < tol, (flags, prec)
