@@ -55,7 +55,9 @@ int pnfft_gb300_set_stream(pnfft_plan ths, void *cuda_stream);
 
 /* Convolution kernels of a plan: 0 = tiled B and line-wise B^T where the
  * cutoff and grid allow (default), 1 = one thread per node (small node
- * counts on large grids).  Chosen per plan, e.g. by timing both. */
+ * counts on large grids), 2 = as 0 but the FP32-mixed B takes one node per
+ * warp instead of groups of nodes with overlapping stencils (the results
+ * are the same bits; for timing).  Chosen per plan, e.g. by timing them. */
 int pnfft_gb300_set_conv_method(pnfft_plan ths, int method);
 int pnfft_gb300_get_conv_method(const pnfft_plan ths);
 

@@ -310,7 +310,7 @@ static int ensure_binning(pnfft_plan p, int64_t M, int spread, int il) {
   DevState::BinSlot &sl = d->bins[spread][il];
   int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
   int T[3], line_mode = 0;
-  choose_tiles(p->cutoff, fp32(p), spread != 0, n, T, &line_mode);
+  choose_tiles(p->cutoff, fp32(p), spread != 0, n, M, T, &line_mode);
   bool same = T[0] == sl.T[0] && T[1] == sl.T[1] && T[2] == sl.T[2] && line_mode == sl.line_mode;
   if (same && sl.cap >= M && sl.b.key && sl.prec == p->precision) return 0;
   int64_t cap = std::max<int64_t>(M, std::max<int64_t>(sl.cap, 1));
@@ -322,23 +322,24 @@ static int ensure_binning(pnfft_plan p, int64_t M, int spread, int il) {
   }
   b.ntiles = b.ntile[0] * b.ntile[1] * b.ntile[2];
   b.line_mode = line_mode;
-  b.sub_max = line_mode ? 2048 : 1024;
-  const int units = line_mode ? b.ntile[0] * b.ntile[1] : b.ntiles;
+  b.nkeys = line_mode == BIN_GROUP ? b.ntiles * kBlocksPerTile : b.ntiles;
+  b.sub_max = line_mode == BIN_LINE ? 2048 : 1024;
+  const int units = line_mode == BIN_LINE ? b.ntile[0] * b.ntile[1] : b.ntiles;
   b.max_subs = (int)(units + cap / b.sub_max + 1);
   PG_CUDA(cudaMalloc(&b.key, sizeof(int) * cap));
   PG_CUDA(cudaMalloc(&b.perm, sizeof(int) * cap));
-  PG_CUDA(cudaMalloc(&b.count, sizeof(int) * b.ntiles));
-  PG_CUDA(cudaMalloc(&b.start, sizeof(int) * b.ntiles));
+  PG_CUDA(cudaMalloc(&b.count, sizeof(int) * b.nkeys));
+  PG_CUDA(cudaMalloc(&b.start, sizeof(int) * b.nkeys));
   PG_CUDA(cudaMalloc(&b.rank, sizeof(int) * cap));
-  PG_CUDA(cudaMalloc(&b.nsub_tile, sizeof(int) * b.ntiles));
-  PG_CUDA(cudaMalloc(&b.sub_off, sizeof(int) * b.ntiles));
+  PG_CUDA(cudaMalloc(&b.nsub_tile, sizeof(int) * b.nkeys));
+  PG_CUDA(cudaMalloc(&b.sub_off, sizeof(int) * b.nkeys));
   PG_CUDA(cudaMalloc(&b.sub_tile, sizeof(int) * b.max_subs));
   PG_CUDA(cudaMalloc(&b.sub_first, sizeof(int) * b.max_subs));
   PG_CUDA(cudaMalloc(&b.sub_cnt, sizeof(int) * b.max_subs));
-  PG_CUDA(cudaMalloc(&b.nsub, sizeof(int)));
+  PG_CUDA(cudaMalloc(&b.nsub, 2 * sizeof(int)));
   PG_CUDA(cudaMalloc(&b.rec, (fp32(p) ? sizeof(float4) : sizeof(double4)) * cap));
   PG_CUDA(cudaMalloc(&b.rec_tmp, (fp32(p) ? sizeof(float4) : sizeof(double4)) * cap));
-  PG_CUDA(cudaMalloc(&b.bsum, sizeof(int) * 2 * ((b.ntiles + 2047) / 2048 + 1)));
+  PG_CUDA(cudaMalloc(&b.bsum, sizeof(int) * 2 * ((b.nkeys + 2047) / 2048 + 1)));
   sl.valid = false;
   sl.cap = cap;
   sl.prec = p->precision;
@@ -686,6 +687,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       memset(&ca, 0, sizeof(ca));
       ca.w = window_args(p);
       ca.generic = p->conv_method == 1;
+      ca.no_group = p->conv_method == 2;
       ca.real_only = p->c2r || (p->pnfft_flags & PNFFT_PRE_QUAD_PSI) ? 1 : 0;
       ca.real_io = p->c2r;
       ca.M = M;
@@ -850,6 +852,7 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       memset(&ca, 0, sizeof(ca));
       ca.w = window_args(p);
       ca.generic = p->conv_method == 1;
+      ca.no_group = p->conv_method == 2;
       ca.real_only = 0;
       ca.real_io = p->c2r;
       ca.M = M;

@@ -1,0 +1,273 @@
+// interp_tile.cuh -- interpolation B with one warp per node over a
+// shared-memory copy of the tile's region; instantiated per precision in
+// interp_tile_f32.cu and interp_tile_f64.cu.
+//
+// Reference: loop_over_particles_trafo / _adj (kernel/ndft-parallel.c:2703-3009)
+// with the stencil loops of kernel/assign.c:478-1159.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+
+#include "pg_conv.cuh"
+#include "pg_kernels.h"
+#include "pg_math.cuh"
+
+namespace pg {
+
+// ---------------------------------------------------------------------------
+// interpolation B, tiled.  The CTA stages its tile's (8+2m)^3 region in
+// shared memory, then walks its nodes in batches: (1) all threads evaluate
+// the window values of the batch (3 x cutoff per node and derivative), (2)
+// one warp per node sums the 13^3 stencil -- lanes (row = lane/16, col =
+// lane%16) read two z-rows of 13 consecutive grid values per step, with the
+// x-window in registers -- and reduces with shuffles, (3) the batch's results
+// are converted and written by all threads.
+// ---------------------------------------------------------------------------
+template <typename T, int CUT, int MODE>
+struct InterpGeom {
+  static constexpr bool DF = (MODE & 1) != 0, DG = (MODE & 2) != 0, DH = (MODE & 4) != 0;
+  static constexpr int NDER = DH ? 2 : (DG ? 1 : 0);
+  static constexpr int R = 8 + CUT - 1, PL = R * R, VOL = R * R * R;
+  static constexpr int NV = 3 * CUT * (NDER + 1);
+  static constexpr int NC = (DF ? 1 : 0) + (DG ? 3 : 0) + (DH ? 6 : 0);
+  static constexpr int NBI = sizeof(T) == 4 ? 48 : 32;
+  static constexpr size_t SMEM = (size_t)VOL * 2 * sizeof(T) + (size_t)NBI * (NV + 2 * NC + 4) * sizeof(T) +
+                                 (size_t)NBI * 2 * sizeof(int);
+};
+
+template <typename T, int CUT, int MODE>
+__global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
+  typedef typename Cplx<T>::type C;
+  typedef InterpGeom<T, CUT, MODE> G;
+  constexpr bool DF = G::DF, DG = G::DG, DH = G::DH;
+  constexpr int NDER = G::NDER, R = G::R, PL = G::PL, VOL = G::VOL, NV = G::NV, NC = G::NC, NBI = G::NBI;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C *reg = (C *)smem_raw;
+  T *s_w = (T *)(reg + VOL);     // [NBI][NV]
+  T *s_res = s_w + NBI * NV;     // [NBI][2*NC]
+  T *s_d = s_res + NBI * 2 * NC; // [NBI][4]
+  int *s_j = (int *)(s_d + NBI * 4);
+  int *s_o = s_j + NBI;
+  const Binning &b = a.bin;
+  const int sub = blockIdx.x;
+  if (sub >= *b.nsub) return;
+  const int tile = b.sub_tile[sub], first = b.sub_first[sub], cnt = b.sub_cnt[sub];
+  if (cnt <= 0) return;  // an empty tile of an ordered sub-problem list
+  int base[3];
+  tile_base(b, tile, base);
+  const int n0 = a.w.n[0], n1 = a.w.n[1], n2 = a.w.n[2];
+  const int tid = threadIdx.x;
+  const C *grid = (const C *)a.grid;
+  load_region<R>(reg, grid, base, n0, n1, n2, a.real_only);
+  const int lane = tid & 31, warp = tid >> 5, nwarp = blockDim.x >> 5;
+  const int row = lane >> 4, col = lane & 15;
+  const T scale = a.use_il ? (T)0.5 : (T)1;
+  for (int b0 = 0; b0 < cnt; b0 += NBI) {
+    const int nb = min(NBI, cnt - b0);
+    __syncthreads();  // region loaded / previous batch flushed
+    for (int i = tid; i < nb; i += blockDim.x) {
+      T d[3];
+      int pk;
+      load_rec_raw(b.rec, first + b0 + i, d, &pk);
+      s_d[4 * i] = d[0];
+      s_d[4 * i + 1] = d[1];
+      s_d[4 * i + 2] = d[2];
+      s_o[i] = pk;
+      s_j[i] = b.perm[first + b0 + i];
+    }
+    __syncthreads();
+    // node-fastest: a warp shares one (axis, stencil point), so the fitted
+    // polynomial rows are broadcast loads
+#pragma unroll 2  // two independent polynomial chains per thread
+    for (int v = tid; v < NBI * 3 * CUT; v += blockDim.x) {
+      const int e = v / NBI, i = v - e * NBI;
+      if (i >= nb) continue;
+      const int t = e / CUT, sidx = e - t * CUT;
+      T out[3];
+      window_point<T>(a.w, t, sidx, s_d[4 * i + t], NDER, out);
+      T *wv = s_w + i * NV;
+      wv[e] = out[0];
+      if (NDER >= 1) wv[3 * CUT + e] = out[1];
+      if (NDER >= 2) wv[6 * CUT + e] = out[2];
+    }
+    __syncthreads();
+    for (int i = warp; i < nb; i += nwarp) {
+      const T *wv = s_w + i * NV;
+      int o[3];
+      unpack_corner(s_o[i], o);
+      T px[CUT], dpx[CUT], ddpx[CUT];
+#pragma unroll
+      for (int l = 0; l < CUT; l++) {
+        px[l] = wv[l];
+        if (NDER >= 1) dpx[l] = wv[3 * CUT + l];
+        if (NDER >= 2) ddpx[l] = wv[6 * CUT + l];
+      }
+      T af_r = 0, af_i = 0;
+      T ag_r[3] = {0, 0, 0}, ag_i[3] = {0, 0, 0};
+      T ah_r[6] = {0, 0, 0, 0, 0, 0}, ah_i[6] = {0, 0, 0, 0, 0, 0};
+      if (col < CUT) {
+        const T pz = wv[2 * CUT + col];
+        const T dz = (NDER >= 1) ? wv[3 * CUT + 2 * CUT + col] : (T)0;
+        const T ddz = (NDER >= 2) ? wv[6 * CUT + 2 * CUT + col] : (T)0;
+        const C *pc = reg + (o[0] * R + o[1]) * R + (o[2] + col);
+#pragma unroll
+        for (int it = 0; it < (CUT + 1) / 2; it++) {
+          const int l1 = 2 * it + row;
+          if (l1 < CUT) {
+            const T py = wv[CUT + l1];
+            const T dy = (NDER >= 1) ? wv[3 * CUT + CUT + l1] : (T)0;
+            const T ddy = (NDER >= 2) ? wv[6 * CUT + CUT + l1] : (T)0;
+            const C *p = pc + l1 * R;
+            T s_r = 0, s_i = 0, sd_r = 0, sd_i = 0, sdd_r = 0, sdd_i = 0;
+#pragma unroll
+            for (int l0 = 0; l0 < CUT; l0++) {
+              const C g = p[l0 * PL];
+              s_r += px[l0] * g.x;
+              s_i += px[l0] * g.y;
+              if (NDER >= 1) {
+                sd_r += dpx[l0] * g.x;
+                sd_i += dpx[l0] * g.y;
+              }
+              if (NDER >= 2) {
+                sdd_r += ddpx[l0] * g.x;
+                sdd_i += ddpx[l0] * g.y;
+              }
+            }
+            const T wyz = py * pz;
+            if (DF) {
+              af_r += wyz * s_r;
+              af_i += wyz * s_i;
+            }
+            if (DG) {
+              ag_r[0] += wyz * sd_r;
+              ag_i[0] += wyz * sd_i;
+              ag_r[1] += dy * pz * s_r;
+              ag_i[1] += dy * pz * s_i;
+              ag_r[2] += py * dz * s_r;
+              ag_i[2] += py * dz * s_i;
+            }
+            if (DH) {
+              ah_r[0] += wyz * sdd_r;
+              ah_i[0] += wyz * sdd_i;
+              ah_r[1] += dy * pz * sd_r;
+              ah_i[1] += dy * pz * sd_i;
+              ah_r[2] += py * dz * sd_r;
+              ah_i[2] += py * dz * sd_i;
+              ah_r[3] += ddy * pz * s_r;
+              ah_i[3] += ddy * pz * s_i;
+              ah_r[4] += dy * dz * s_r;
+              ah_i[4] += dy * dz * s_i;
+              ah_r[5] += py * ddz * s_r;
+              ah_i[5] += py * ddz * s_i;
+            }
+          }
+        }
+      }
+      T *res = s_res + i * 2 * NC;
+      int c = 0;
+      if (DF) {
+        T r = warp_sum(af_r), im = warp_sum(af_i);
+        if (lane == 0) {
+          res[0] = r * scale;
+          res[1] = im * scale;
+        }
+        c = 1;
+      }
+      if (DG) {
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          T r = warp_sum(ag_r[k]), im = warp_sum(ag_i[k]);
+          if (lane == 0) {
+            res[2 * (c + k)] = r * scale;
+            res[2 * (c + k) + 1] = im * scale;
+          }
+        }
+      }
+      if (DH) {
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+          T r = warp_sum(ah_r[k]), im = warp_sum(ah_i[k]);
+          if (lane == 0) {
+            res[2 * k] = r * scale;
+            res[2 * k + 1] = im * scale;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // write the batch: one thread per (node, output component)
+    for (int v = tid; v < nb * NC; v += blockDim.x) {
+      const int i = v / NC, k = v - i * NC;
+      const int64_t ind = (int64_t)s_j[i] * a.stride + a.offset;
+      double *out;
+      int64_t e;
+      if (DH) {
+        out = a.hess_out;
+        e = 6 * ind + k;
+      } else if (DF && k == 0) {
+        out = a.f_out;
+        e = ind;
+      } else {
+        out = a.grad_out;
+        e = 3 * ind + (k - (DF ? 1 : 0));
+      }
+      const double vr = (double)s_res[i * 2 * NC + 2 * k], vi = (double)s_res[i * 2 * NC + 2 * k + 1];
+      if (a.real_io) {
+        if (a.accum) out[e] += vr;
+        else out[e] = vr;
+      } else {
+        double2 *o2 = (double2 *)out + e;
+        if (a.accum) {
+          double2 t = *o2;
+          t.x += vr;
+          t.y += vi;
+          *o2 = t;
+        } else {
+          *o2 = make_double2(vr, vi);
+        }
+      }
+    }
+  }
+}
+
+template <typename T, int CUT, int MODE>
+static void run_interp_tile(const ConvArgs &a, cudaStream_t s) {
+  const size_t sm = InterpGeom<T, CUT, MODE>::SMEM;
+  // the shared-memory opt-in is a per-device attribute of the kernel
+  static std::atomic<unsigned long long> attr_done{0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(attr_done.load() & bit)) {
+    cudaFuncSetAttribute(k_interp_tile<T, CUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    attr_done.fetch_or(bit);
+  }
+  k_interp_tile<T, CUT, MODE><<<a.bin.max_subs, 256, sm, s>>>(a);
+}
+
+template <typename T, int MODE>
+static bool interp_tile_by_cut(const ConvArgs &a, cudaStream_t s) {
+  switch (a.w.cut) {
+    case 5: run_interp_tile<T, 5, MODE>(a, s); return true;
+    case 7: run_interp_tile<T, 7, MODE>(a, s); return true;
+    case 9: run_interp_tile<T, 9, MODE>(a, s); return true;
+    case 11: run_interp_tile<T, 11, MODE>(a, s); return true;
+    case 13: run_interp_tile<T, 13, MODE>(a, s); return true;
+    case 15: run_interp_tile<T, 15, MODE>(a, s); return true;
+    default: return false;
+  }
+}
+
+template <typename T>
+static bool interp_tile_t(const ConvArgs &a, int mode, cudaStream_t s) {
+  switch (mode) {
+    case 1: return interp_tile_by_cut<T, 1>(a, s);
+    case 2: return interp_tile_by_cut<T, 2>(a, s);
+    case 3: return interp_tile_by_cut<T, 3>(a, s);
+    case 4: return interp_tile_by_cut<T, 4>(a, s);
+    default: return false;
+  }
+}
+
+}  // namespace pg

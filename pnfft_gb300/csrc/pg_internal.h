@@ -39,7 +39,8 @@ struct pnfft_plan_s {
   double timer_adj[PNFFT_TIMER_LENGTH];
   double last_ms[2][PNFFT_TIMER_LENGTH];
   int precision;      // PNFFT_GB300_FP64 / PNFFT_GB300_FP32_MIXED
-  int conv_method;    // 0: tiled/line kernels where usable, 1: one thread per node
+  int conv_method;    // 0: tiled/line kernels where usable, 1: one thread per node,
+                      // 2: tiled without node groups in the FP32-mixed interpolation
   void *d_f_hat_user; // zero-copy f_hat
   void *user_stream;
   uint64_t uid;

@@ -32,25 +32,37 @@ constexpr int kPolyCoef = 16;
 // of the nodes of one line of tiles along axis 2 (the tiles with the same
 // t0, t1, which the sort keeps consecutive and in slab order), and the
 // records carry the full lowest z index u2 instead of the in-tile offset.
+// In group mode (FP32-mixed interpolation) the sort key is finer: the tile
+// and the 2x2x4 block of stencil corners within it (32 keys per tile), and
+// the record of every kGroupMax-th node of a block (by rank) carries a
+// group-start bit, so that the nodes of one block are consecutive and cut
+// into groups of at most kGroupMax nodes whose stencils overlap.
+enum BinMode { BIN_TILE = 0, BIN_LINE = 1, BIN_GROUP = 2 };
+constexpr int kBlocksPerTile = 32;  // 2x2x4 corner blocks of an 8x8x8 tile
+constexpr int kGroupMax = 4;        // nodes of one block interpolated together
+constexpr int kGroupBit = 1 << 24;  // record flag: first node of a group
+constexpr int kGroupSubMax = 1024;  // nodes per sub-problem of the grouped interpolation
+
 struct Binning {
   int T[3], ntile[3];
   int ntiles, sub_max, max_subs;
-  int line_mode;
-  int *key;        // [M] tile of each node
-  int *perm;       // [M] nodes sorted by tile
-  int *count;      // [ntiles]
-  int *start;      // [ntiles]
-  int *rank;       // [M] position of each node within its tile
-  int *nsub_tile;  // [ntiles]
-  int *sub_off;    // [ntiles]
+  int line_mode;   // BinMode
+  int nkeys;       // sort keys: ntiles, or ntiles * kBlocksPerTile in group mode
+  int *key;        // [M] sort key of each node
+  int *perm;       // [M] nodes sorted by key
+  int *count;      // [nkeys]
+  int *start;      // [nkeys]
+  int *rank;       // [M] position of each node within its key
+  int *nsub_tile;  // [nkeys]
+  int *sub_off;    // [nkeys]
   int *sub_tile;   // [max_subs]
   int *sub_first;  // [max_subs]
   int *sub_cnt;    // [max_subs]
-  int *nsub;       // [1]
+  int *nsub;       // [2] sub-problem count; [1]: runs beyond the first per unit (group mode)
   void *rec;       // [M] node records in tile order: float4 (FP32-mixed) or double4
                    // {dist0, dist1, dist2, local stencil corner o0 | o1<<8 | o2<<16}
   void *rec_tmp;   // [M] the same records in node order (before the scatter)
-  int *bsum;       // [2 * ceil(ntiles / 2048)] scan block sums
+  int *bsum;       // [2 * ceil(nkeys / 2048)] scan block sums
 };
 
 // One convolution (B or B^T) launch.
@@ -62,6 +74,7 @@ struct ConvArgs {
   int real_io;      // node arrays are real (c2r) instead of complex
   int accum;        // add into the node outputs (else store): ACCUMULATED, 2nd interlaced pass
   int generic;      // use the one-thread-per-node kernels (set per plan, e.g. by an autotuner)
+  int no_group;     // FP32-mixed interpolation: one warp per node also on a group-mode binning
   int64_t M;
   const double *x;  // [M][3]
   void *grid;       // n0*n1*n2 complex in compute precision, natural order
@@ -77,9 +90,22 @@ struct ConvArgs {
 void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s);
 void launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
 void launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
-// Tile shape of the binning for interpolation (spread = false) or spreading
-// (spread = true); *line_mode is set for the line-of-tiles spreading.
-void choose_tiles(int cut, bool fp32, bool spread, const int *n, int *T, int *line_mode);
+// Kernel families behind launch_interp / launch_spread; each returns false
+// when it has no instance for the cutoff or mode.
+// FP32-mixed f-only interpolation on a BIN_GROUP binning (interp_group.cu)
+bool launch_interp_group(const ConvArgs &a, cudaStream_t s);
+// one warp per node on tile binnings (interp_tile_f32.cu, interp_tile_f64.cu)
+bool launch_interp_tile_f32(const ConvArgs &a, int mode, cudaStream_t s);
+bool launch_interp_tile_f64(const ConvArgs &a, int mode, cudaStream_t s);
+// lines of tiles (spread_line_f32.cu, spread_line_f64.cu)
+bool launch_spread_line_f32(const ConvArgs &a, int mode, cudaStream_t s);
+bool launch_spread_line_f64(const ConvArgs &a, int mode, cudaStream_t s);
+// one thread per node, any cutoff (generic.cu)
+void launch_interp_generic(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
+void launch_spread_generic(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
+// Tile shape and BinMode of the binning for interpolation (spread = false)
+// or spreading (spread = true).
+void choose_tiles(int cut, bool fp32, bool spread, const int *n, int64_t M, int *T, int *line_mode);
 
 // Deconvolution (deconv.cu).
 struct DeconvArgs {

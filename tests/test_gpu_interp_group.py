@@ -1,0 +1,137 @@
+"""The grouped FP32-mixed interpolation.
+
+On grids with enough nodes (half a node per 2x2x4 block of stencil corners
+or more) the FP32-mixed trafo with f only interpolates the nodes of one
+block in groups of up to four per warp.  Its sums are the ones of the
+one-node-per-warp kernel term by term, so conv method 0 (grouped) and
+method 2 (one node per warp on the same binning) give the same bits; both
+match the oracle within the FP32-mixed tolerance.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+WINDOWS = {
+    "kaiser_bessel": 0,
+    "gaussian": 1 << 13,
+    "bspline": 1 << 14,
+    "sinc_power": 1 << 15,
+    "bessel_i0": 1 << 16,
+    "gaussian_t": (1 << 17) | (1 << 13),
+}
+
+
+def rel(a, b):
+    d = np.linalg.norm((np.asarray(a) - np.asarray(b)).ravel())
+    nb = np.linalg.norm(np.asarray(b).ravel())
+    return d / nb if nb > 0 else d
+
+
+@pytest.fixture(scope="module")
+def gpu(lib):
+    if lib.device_count() == 0:
+        pytest.fail("no CUDA device visible for a -m gpu test")
+    return lib
+
+
+def spectrum(rng, p):
+    S = int(np.prod(p.local_N))
+    return rng.standard_normal(S) + 1j * rng.standard_normal(S)
+
+
+def both_methods(gpu, N, x, m, flags=0, c2r=False, cflags=1, f0=None, seed=0):
+    """trafo (f only) with the grouped kernel and with one node per warp."""
+    out = []
+    for method in (0, 2):
+        p = gpu.Plan(N, m=m, flags=flags, precision="fp32", c2r=c2r)
+        p.set_conv_method(method)
+        fh = spectrum(np.random.default_rng(seed), p)
+        kw = {} if f0 is None else {"f": f0.copy()}
+        out.append(p.trafo(x, fh, cflags, **kw)[0].copy())
+        p.close()
+    return out
+
+
+@pytest.mark.parametrize("win", list(WINDOWS))
+@pytest.mark.parametrize("m", [2, 3, 4, 5, 6, 7])  # m = 7: cutoff 15 is not grouped
+def test_grouped_same_bits_as_per_node(gpu, win, m):
+    N = (16, 16, 16)  # n = 32^3: 64 tiles, 2048 corner blocks
+    x = np.random.default_rng(100 + m).uniform(-0.5, 0.5, (3000, 3))
+    a, b = both_methods(gpu, N, x, m, flags=WINDOWS[win], seed=m)
+    assert np.isfinite(a).all()
+    np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("case", ["interlaced", "pre_lin_psi", "pre_cub_psi", "accumulated", "c2r", "odd_grid",
+                                  "clustered", "boundary_nodes"])
+def test_grouped_same_bits_variants(gpu, case):
+    rng = np.random.default_rng(7)
+    N, m, flags, c2r, f0 = (16, 16, 16), 6, 0, False, None
+    M = 4000
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    if case == "interlaced":
+        flags = gpu.INTERLACED
+    elif case == "pre_lin_psi":
+        flags = gpu.PRE_LIN_PSI
+    elif case == "pre_cub_psi":
+        flags = gpu.PRE_CUB_PSI
+    elif case == "accumulated":
+        f0 = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+    elif case == "c2r":
+        c2r = True
+        f0 = None
+    elif case == "odd_grid":
+        N = (12, 18, 14)  # n = 24 x 36 x 28: tiles that wrap
+    elif case == "clustered":
+        # dense clusters: sub-problems of 1024 nodes split blocks and groups
+        x = np.concatenate([x[:500], 0.1 + 0.001 * rng.standard_normal((6000, 3)),
+                            -0.3 + 0.0004 * rng.standard_normal((3000, 3))])
+    elif case == "boundary_nodes":
+        # nodes on cell boundaries and at the ends of the torus
+        g = np.arange(-16, 16) / 32.0
+        x = np.stack(np.meshgrid(g, g[::3], g[::2], indexing="ij"), -1).reshape(-1, 3)
+        x = np.concatenate([x, np.full((64, 3), -0.5), np.full((64, 3), 0.5 - 2.0 ** -40)])
+    cflags = 1 | (gpu.COMPUTE_ACCUMULATED if f0 is not None else 0)
+    a, b = both_methods(gpu, N, x, m, flags=flags, c2r=c2r, cflags=cflags, f0=f0, seed=3)
+    assert np.isfinite(a).all()
+    np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("win", ["kaiser_bessel", "bessel_i0", "bspline"])
+def test_grouped_vs_oracle(gpu, oracle, win):
+    N = (16, 16, 16)
+    rng = np.random.default_rng(21)
+    x = rng.uniform(-0.5, 0.5, (3000, 3))
+    p = gpu.Plan(N, m=6, flags=WINDOWS[win], precision="fp32")
+    o = oracle.OraclePlan(N, m=6, flags=WINDOWS[win])
+    fh = spectrum(rng, p)
+    assert rel(p.trafo(x, fh)[0], o.trafo(x, fh)[0]) < 2e-6
+
+
+def test_grouped_kernel_runs(gpu):
+    # the grouped kernel is the one launched for this workload (and not for
+    # method 2 or a gradient request)
+    torch = pytest.importorskip("torch")
+    from torch.profiler import ProfilerActivity, profile
+
+    N = (16, 16, 16)
+    x = np.random.default_rng(5).uniform(-0.5, 0.5, (3000, 3))
+
+    def kernels(method, cflags):
+        p = gpu.Plan(N, m=6, precision="fp32")
+        p.set_conv_method(method)
+        fh = spectrum(np.random.default_rng(1), p)
+        p.trafo(x, fh, cflags)  # binning and attributes outside the profile
+        with profile(activities=[ProfilerActivity.CUDA]) as prof:
+            p.trafo(x, fh, cflags)
+            torch.cuda.synchronize()
+        p.close()
+        return " ".join(e.name for e in prof.events())
+
+    names = kernels(0, 1)
+    if "k_" not in names:
+        pytest.skip("the profiler recorded no kernels")
+    assert "k_interp_group" in names
+    assert "k_interp_group" not in kernels(2, 1)
+    assert "k_interp_group" not in kernels(0, 1 | 2)
