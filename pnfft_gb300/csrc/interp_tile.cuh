@@ -103,9 +103,8 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
         if (NDER >= 1) dpx[l] = wv[3 * CUT + l];
         if (NDER >= 2) ddpx[l] = wv[6 * CUT + l];
       }
-      T af_r = 0, af_i = 0;
-      T ag_r[3] = {0, 0, 0}, ag_i[3] = {0, 0, 0};
-      T ah_r[6] = {0, 0, 0, 0, 0, 0}, ah_i[6] = {0, 0, 0, 0, 0, 0};
+      const C zero = {(T)0, (T)0};
+      C af = zero, ag[3] = {zero, zero, zero}, ah[6] = {zero, zero, zero, zero, zero, zero};
       if (col < CUT) {
         const T pz = wv[2 * CUT + col];
         const T dz = (NDER >= 1) ? wv[3 * CUT + 2 * CUT + col] : (T)0;
@@ -119,47 +118,28 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
             const T dy = (NDER >= 1) ? wv[3 * CUT + CUT + l1] : (T)0;
             const T ddy = (NDER >= 2) ? wv[6 * CUT + CUT + l1] : (T)0;
             const C *p = pc + l1 * R;
-            T s_r = 0, s_i = 0, sd_r = 0, sd_i = 0, sdd_r = 0, sdd_i = 0;
+            C sx = zero, sd = zero, sdd = zero;
 #pragma unroll
             for (int l0 = 0; l0 < CUT; l0++) {
               const C g = p[l0 * PL];
-              s_r += px[l0] * g.x;
-              s_i += px[l0] * g.y;
-              if (NDER >= 1) {
-                sd_r += dpx[l0] * g.x;
-                sd_i += dpx[l0] * g.y;
-              }
-              if (NDER >= 2) {
-                sdd_r += ddpx[l0] * g.x;
-                sdd_i += ddpx[l0] * g.y;
-              }
+              cfma(sx, px[l0], g);
+              if (NDER >= 1) cfma(sd, dpx[l0], g);
+              if (NDER >= 2) cfma(sdd, ddpx[l0], g);
             }
             const T wyz = py * pz;
-            if (DF) {
-              af_r += wyz * s_r;
-              af_i += wyz * s_i;
-            }
+            if (DF) cfma(af, wyz, sx);
             if (DG) {
-              ag_r[0] += wyz * sd_r;
-              ag_i[0] += wyz * sd_i;
-              ag_r[1] += dy * pz * s_r;
-              ag_i[1] += dy * pz * s_i;
-              ag_r[2] += py * dz * s_r;
-              ag_i[2] += py * dz * s_i;
+              cfma(ag[0], wyz, sd);
+              cfma(ag[1], dy * pz, sx);
+              cfma(ag[2], py * dz, sx);
             }
             if (DH) {
-              ah_r[0] += wyz * sdd_r;
-              ah_i[0] += wyz * sdd_i;
-              ah_r[1] += dy * pz * sd_r;
-              ah_i[1] += dy * pz * sd_i;
-              ah_r[2] += py * dz * sd_r;
-              ah_i[2] += py * dz * sd_i;
-              ah_r[3] += ddy * pz * s_r;
-              ah_i[3] += ddy * pz * s_i;
-              ah_r[4] += dy * dz * s_r;
-              ah_i[4] += dy * dz * s_i;
-              ah_r[5] += py * ddz * s_r;
-              ah_i[5] += py * ddz * s_i;
+              cfma(ah[0], wyz, sdd);
+              cfma(ah[1], dy * pz, sd);
+              cfma(ah[2], py * dz, sd);
+              cfma(ah[3], ddy * pz, sx);
+              cfma(ah[4], dy * dz, sx);
+              cfma(ah[5], py * ddz, sx);
             }
           }
         }
@@ -167,7 +147,7 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
       T *res = s_res + i * 2 * NC;
       int c = 0;
       if (DF) {
-        T r = warp_sum(af_r), im = warp_sum(af_i);
+        T r = warp_sum(af.x), im = warp_sum(af.y);
         if (lane == 0) {
           res[0] = r * scale;
           res[1] = im * scale;
@@ -177,7 +157,7 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
       if (DG) {
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-          T r = warp_sum(ag_r[k]), im = warp_sum(ag_i[k]);
+          T r = warp_sum(ag[k].x), im = warp_sum(ag[k].y);
           if (lane == 0) {
             res[2 * (c + k)] = r * scale;
             res[2 * (c + k) + 1] = im * scale;
@@ -187,7 +167,7 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
       if (DH) {
 #pragma unroll
         for (int k = 0; k < 6; k++) {
-          T r = warp_sum(ah_r[k]), im = warp_sum(ah_i[k]);
+          T r = warp_sum(ah[k].x), im = warp_sum(ah[k].y);
           if (lane == 0) {
             res[2 * k] = r * scale;
             res[2 * k + 1] = im * scale;

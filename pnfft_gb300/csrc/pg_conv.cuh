@@ -69,6 +69,14 @@ __device__ __forceinline__ void tile_base(const Binning &b, int tile, int *base)
   base[2] = t2 * b.T[2];
 }
 
+// acc += w * g for a complex g and a real weight w: the paired FMA of sm_100+
+// in FP32 (each component rounds like fmaf), two FMAs in FP64
+__device__ __forceinline__ void cfma(float2 &acc, float w, float2 g) { acc = __ffma2_rn(make_float2(w, w), g, acc); }
+__device__ __forceinline__ void cfma(double2 &acc, double w, double2 g) {
+  acc.x = fma(w, g.x, acc.x);
+  acc.y = fma(w, g.y, acc.y);
+}
+
 // copies the R^3 region of the grid starting at base (wrapped modulo n) into
 // shared memory, row-major with z fastest; R even.  FP32 grids with even n2
 // move two complex values per 16-byte load (pairs never straddle the wrap:

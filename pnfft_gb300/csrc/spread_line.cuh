@@ -83,6 +83,16 @@ __device__ __forceinline__ void commit_pair(double2 *col, int z, int n2, bool, d
   if (r1 != 0.0 || i1 != 0.0) atomic_add_grid(col + (z + 1) % n2, make_double2(r1, i1));
 }
 
+// acc += (hr + i hi) * p: the paired FMA of sm_100+ in FP32 (each component
+// rounds like fmaf), two FMAs in FP64
+__device__ __forceinline__ void acc_fma(float2 &acc, float hr, float hi, float p) {
+  acc = __ffma2_rn(make_float2(hr, hi), make_float2(p, p), acc);
+}
+__device__ __forceinline__ void acc_fma(double2 &acc, double hr, double hi, double p) {
+  acc.x = fma(hr, p, acc.x);
+  acc.y = fma(hi, p, acc.y);
+}
+
 template <typename T, int CUT, int MODE>
 __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1) k_spread_line(ConvArgs a) {
   typedef typename Cplx<T>::type C;
@@ -110,11 +120,12 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
   const size_t gx = (size_t)((t0 * TL + ca) % n0) * n1;
   C *col[2] = {(C *)a.grid + (gx + (t1 * TL + cb) % n1) * n2, (C *)a.grid + (gx + (t1 * TL + cb + HR) % n1) * n2};
   const bool vec = (n2 & 1) == 0;
-  T acc_r[2][W], acc_i[2][W];
+  C acc[2][W];  // the two columns' z windows (re, im)
+  const C zero = {(T)0, (T)0};
 #pragma unroll
   for (int c = 0; c < 2; c++)
 #pragma unroll
-    for (int z = 0; z < W; z++) acc_r[c][z] = acc_i[c][z] = (T)0;
+    for (int z = 0; z < W; z++) acc[c][z] = zero;
   int zslab = -1, since = 0;
   const T scale = a.use_il ? (T)0.5 : (T)1;
   // commit values [z0, z1) of both columns at grid z = zb + z
@@ -124,7 +135,7 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
 #pragma unroll
       for (int z = 0; z < W; z += 2)
         if (z >= z0 && z < z1)
-          commit_pair(col[c], zb + z, n2, vec, acc_r[c][z], acc_i[c][z], acc_r[c][z + 1], acc_i[c][z + 1]);
+          commit_pair(col[c], zb + z, n2, vec, acc[c][z].x, acc[c][z].y, acc[c][z + 1].x, acc[c][z + 1].y);
   };
   for (int b0 = 0; b0 < cnt; b0 += NB) {
     const int nb = min(NB, cnt - b0);
@@ -190,7 +201,7 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
 #pragma unroll
       for (int c = 0; c < 2; c++)
 #pragma unroll
-        for (int z = 0; z < W; z++) acc_r[c][z] = acc_i[c][z] = (T)0;
+        for (int z = 0; z < W; z++) acc[c][z] = zero;
       since = 0;
     }
 #pragma unroll 2
@@ -205,19 +216,16 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
 #pragma unroll
             for (int c = 0; c < 2; c++)
 #pragma unroll
-              for (int z = 0; z < W; z++) acc_r[c][z] = acc_i[c][z] = (T)0;
+              for (int z = 0; z < W; z++) acc[c][z] = zero;
           } else {
             for (int q = 0; q < steps; q++) {
               commit((zslab + q) * TL, 0, TL);
 #pragma unroll
               for (int c = 0; c < 2; c++) {
 #pragma unroll
-                for (int z = 0; z < W - TL; z++) {
-                  acc_r[c][z] = acc_r[c][z + TL];
-                  acc_i[c][z] = acc_i[c][z + TL];
-                }
+                for (int z = 0; z < W - TL; z++) acc[c][z] = acc[c][z + TL];
 #pragma unroll
-                for (int z = W - TL; z < W; z++) acc_r[c][z] = acc_i[c][z] = (T)0;
+                for (int z = W - TL; z < W; z++) acc[c][z] = zero;
               }
             }
           }
@@ -265,17 +273,11 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
               h1i += g0i * py + g1i * dpy;
             }
 #pragma unroll
-            for (int z = 0; z < W; z++) {
-              acc_r[c][z] += h1r * pz[z];
-              acc_i[c][z] += h1i * pz[z];
-            }
+            for (int z = 0; z < W; z++) acc_fma(acc[c][z], h1r, h1i, pz[z]);
             if (DG) {
               const T h2r = g2r * py, h2i = g2i * py;
 #pragma unroll
-              for (int z = 0; z < W; z++) {
-                acc_r[c][z] += h2r * dz[z];
-                acc_i[c][z] += h2i * dz[z];
-              }
+              for (int z = 0; z < W; z++) acc_fma(acc[c][z], h2r, h2i, dz[z]);
             }
           }
         }
