@@ -226,7 +226,7 @@ __global__ void k_bin_subs(Binning b) {
 // (a line of tiles along axis 2, or the corner blocks of one tile); thread per
 // unit.  `ordered`: sub-problem L is the first run of unit L (empty when the
 // unit has no nodes) and further runs follow the nunits slots, so that CTAs
-// take tiles in grid order (neighbours share their halos in L2)
+// take tiles / lines in grid order (neighbours share their halos in L2)
 __global__ void k_bin_group_subs(Binning b, int64_t M, int group, int nunits, int ordered) {
   const int L = blockIdx.x * blockDim.x + threadIdx.x;
   if (L >= nunits) return;
@@ -281,7 +281,7 @@ void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s) {
     const int group = line ? b.ntile[2] : kBlocksPerTile;
     const int nunits = line ? b.ntile[0] * b.ntile[1] : b.ntiles;
     cudaMemsetAsync(b.nsub, 0, 2 * sizeof(int), s);
-    k_bin_group_subs<<<(nunits + 255) / 256, 256, 0, s>>>(b, a.M, group, nunits, line ? 0 : 1);
+    k_bin_group_subs<<<(nunits + 255) / 256, 256, 0, s>>>(b, a.M, group, nunits, 1);
   } else {
     k_bin_subs<<<(b.nkeys + 255) / 256, 256, 0, s>>>(b);
   }

@@ -77,31 +77,36 @@ __device__ __forceinline__ void group_sums(const ConvArgs &a, const float2 *__re
   for (int k = 0; k < G; k++) af[k] = make_float2(0.f, 0.f);
   const bool active = col < CUT + dz;
   const float2 *pc = reg + (x0 * R + y0) * R + (z0 + col);
-  // the row loop stays rolled: four group sizes of unrolled rows would not
-  // fit the instruction cache
+  // the row loop stays rolled (instruction cache)
 #pragma unroll 1
   for (int it = 0; it < (CUT + 2) / 2; it++) {
     const int Y = 2 * it + row;  // row of the union
     if (active && Y < CUT + dy) {
       const float2 *p = pc + Y * R;
-      float2 sx[G];
+      // union planes of even and odd L in separate chains: for each node
+      // these are its even and odd x planes (in one order or the other, with
+      // exact zeros at the ends), as the chains of k_interp_tile; their sum
+      // does not depend on the order
+      float2 sp[2][G];
 #pragma unroll
-      for (int k = 0; k < G; k++) sx[k] = make_float2(0.f, 0.f);
+      for (int k = 0; k < G; k++) sp[0][k] = sp[1][k] = make_float2(0.f, 0.f);
 #pragma unroll
       for (int L = 0; L < CUT; L++) {
         const float2 g = p[L * PL];
 #pragma unroll
-        for (int k = 0; k < G; k++) sx[k] = __ffma2_rn(make_float2(px[k][L], px[k][L]), g, sx[k]);
+        for (int k = 0; k < G; k++) sp[L & 1][k] = __ffma2_rn(make_float2(px[k][L], px[k][L]), g, sp[L & 1][k]);
       }
       if (dx) {
         const float2 g = p[CUT * PL];
 #pragma unroll
-        for (int k = 0; k < G; k++) sx[k] = __ffma2_rn(make_float2(px[k][CUT], px[k][CUT]), g, sx[k]);
+        for (int k = 0; k < G; k++)
+          sp[CUT & 1][k] = __ffma2_rn(make_float2(px[k][CUT], px[k][CUT]), g, sp[CUT & 1][k]);
       }
 #pragma unroll
       for (int k = 0; k < G; k++) {
+        const float2 sx = cadd(sp[0][k], sp[1][k]);
         const float wyz = wv[k * NW + 16 + Y] * pz[k];
-        af[k] = __ffma2_rn(make_float2(wyz, wyz), sx[k], af[k]);
+        af[k] = __ffma2_rn(make_float2(wyz, wyz), sx, af[k]);
       }
     }
   }
@@ -235,9 +240,8 @@ __global__ void __launch_bounds__(256, 2) k_interp_group(ConvArgs a) {
       oz[k] -= z0;
     }
     // window values, shifted into zeroed slots (also the slots of the
-    // zero-weight nodes that pad a group to the kernel's size)
-    const int gk = g <= 2 ? 2 : kGroupMax;
-    for (int v = lane; v < gk * (NW / 4); v += 32) ((float4 *)wv)[v] = make_float4(0.f, 0.f, 0.f, 0.f);
+    // zero-weight nodes that pad a group to kGroupMax)
+    for (int v = lane; v < kGroupMax * (NW / 4); v += 32) ((float4 *)wv)[v] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncwarp();
     if (poly) {
       // lane e: stencil point e % CUT of axis e / CUT for all nodes of the group
@@ -274,9 +278,9 @@ __global__ void __launch_bounds__(256, 2) k_interp_group(ConvArgs a) {
     }
     __syncwarp();
     const int dx = x1 - x0, dy = y1 - y0, dz = z1 - z0;  // <= 1, 1, 3
-    // two sizes of the sums keep the code small; groups of 1 and 3 are padded
-    if (gk == 2) group_sums<CUT, 2>(a, reg, wv, ox, oy, oz, x0, y0, z0, dx, dy, dz, g, lane, jn, scale);
-    else group_sums<CUT, kGroupMax>(a, reg, wv, ox, oy, oz, x0, y0, z0, dx, dy, dz, g, lane, jn, scale);
+    // one size of the sums keeps the hot code in the instruction cache;
+    // smaller groups are padded with zero-weight nodes
+    group_sums<CUT, kGroupMax>(a, reg, wv, ox, oy, oz, x0, y0, z0, dx, dy, dz, g, lane, jn, scale);
     __syncwarp();  // the group's slots are free
   }
 }

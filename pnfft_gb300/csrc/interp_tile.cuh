@@ -118,14 +118,19 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
             const T dy = (NDER >= 1) ? wv[3 * CUT + CUT + l1] : (T)0;
             const T ddy = (NDER >= 2) ? wv[6 * CUT + CUT + l1] : (T)0;
             const C *p = pc + l1 * R;
-            C sx = zero, sd = zero, sdd = zero;
+            // even and odd x planes in separate chains (independent FMAs),
+            // added at the end of the row
+            C sxp[2] = {zero, zero}, sdp[2] = {zero, zero}, sddp[2] = {zero, zero};
 #pragma unroll
             for (int l0 = 0; l0 < CUT; l0++) {
               const C g = p[l0 * PL];
-              cfma(sx, px[l0], g);
-              if (NDER >= 1) cfma(sd, dpx[l0], g);
-              if (NDER >= 2) cfma(sdd, ddpx[l0], g);
+              cfma(sxp[l0 & 1], px[l0], g);
+              if (NDER >= 1) cfma(sdp[l0 & 1], dpx[l0], g);
+              if (NDER >= 2) cfma(sddp[l0 & 1], ddpx[l0], g);
             }
+            const C sx = cadd(sxp[0], sxp[1]);
+            const C sd = NDER >= 1 ? cadd(sdp[0], sdp[1]) : zero;
+            const C sdd = NDER >= 2 ? cadd(sddp[0], sddp[1]) : zero;
             const T wyz = py * pz;
             if (DF) cfma(af, wyz, sx);
             if (DG) {

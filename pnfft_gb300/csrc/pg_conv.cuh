@@ -76,6 +76,8 @@ __device__ __forceinline__ void cfma(double2 &acc, double w, double2 g) {
   acc.x = fma(w, g.x, acc.x);
   acc.y = fma(w, g.y, acc.y);
 }
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 
 // copies the R^3 region of the grid starting at base (wrapped modulo n) into
 // shared memory, row-major with z fastest; R even.  FP32 grids with even n2

@@ -112,6 +112,7 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
   const int sub = blockIdx.x;
   if (sub >= *b.nsub) return;
   const int line = b.sub_tile[sub], first = b.sub_first[sub], cnt = b.sub_cnt[sub];
+  if (cnt <= 0) return;  // a line without nodes
   const int t1 = line % b.ntile[1], t0 = line / b.ntile[1];
   const int tid = threadIdx.x, nth = blockDim.x;
   const bool active = tid < R * HR;
