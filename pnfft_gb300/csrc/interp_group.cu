@@ -110,32 +110,56 @@ __device__ __forceinline__ void group_sums(const ConvArgs &a, const float2 *__re
       }
     }
   }
-  // move each node's partial sums to the lanes of k_interp_tile, reduce, and
-  // let lane k write node k (nodes k >= g pad the group)
+  // move each node's partial sums to the lanes of k_interp_tile, then reduce
+  // the 2G values together: at each xor distance (16, 8, 4, then 2 and 1)
+  // a lane keeps half of its values and adds the partner's copies, so every
+  // value sees the pairs of warp_sum, and ends in the lanes whose bits 4..2
+  // give its index (2k: re, 2k + 1: im of node k)
+  static_assert(G == 4, "the transposed reduction is written for 8 values");
+  float v[2 * G];
 #pragma unroll
   for (int k = 0; k < G; k++) {
-    if (k >= g) break;
     const int src = (((row + oy[k]) & 1) << 4) + col + oz[k];
-    float r = __shfl_sync(0xffffffffu, af[k].x, src & 31), im = __shfl_sync(0xffffffffu, af[k].y, src & 31);
-    if (col >= CUT) r = im = 0.f;
-    r = warp_sum(r);
-    im = warp_sum(im);
-    if (lane == k) {
-      const int64_t e = (int64_t)jn * a.stride + a.offset;
-      const double vr = (double)(r * scale), vi = (double)(im * scale);
-      if (a.real_io) {
-        if (a.accum) a.f_out[e] += vr;
-        else a.f_out[e] = vr;
+    v[2 * k] = __shfl_sync(0xffffffffu, af[k].x, src & 31);
+    v[2 * k + 1] = __shfl_sync(0xffffffffu, af[k].y, src & 31);
+    if (col >= CUT) v[2 * k] = v[2 * k + 1] = 0.f;
+  }
+  const bool b4 = lane & 16, b3 = lane & 8, b2 = lane & 4;
+  float u[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const float send = b4 ? v[j] : v[4 + j];
+    const float keep = b4 ? v[4 + j] : v[j];
+    u[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+  }
+  float w2[2];
+#pragma unroll
+  for (int j = 0; j < 2; j++) {
+    const float send = b3 ? u[j] : u[2 + j];
+    const float keep = b3 ? u[2 + j] : u[j];
+    w2[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+  }
+  float x = (b2 ? w2[1] : w2[0]) + __shfl_xor_sync(0xffffffffu, b2 ? w2[0] : w2[1], 4);
+  x += __shfl_xor_sync(0xffffffffu, x, 2);
+  x += __shfl_xor_sync(0xffffffffu, x, 1);
+  // lane k < g writes node k: re from lane 8k, im from lane 8k + 4
+  const float r = __shfl_sync(0xffffffffu, x, (8 * lane) & 31);
+  const float im = __shfl_sync(0xffffffffu, x, (8 * lane + 4) & 31);
+  if (lane < g) {
+    const int64_t e = (int64_t)jn * a.stride + a.offset;
+    const double vr = (double)(r * scale), vi = (double)(im * scale);
+    if (a.real_io) {
+      if (a.accum) a.f_out[e] += vr;
+      else a.f_out[e] = vr;
+    } else {
+      double2 *o2 = (double2 *)a.f_out + e;
+      if (a.accum) {
+        double2 t = *o2;
+        t.x += vr;
+        t.y += vi;
+        *o2 = t;
       } else {
-        double2 *o2 = (double2 *)a.f_out + e;
-        if (a.accum) {
-          double2 t = *o2;
-          t.x += vr;
-          t.y += vi;
-          *o2 = t;
-        } else {
-          *o2 = make_double2(vr, vi);
-        }
+        *o2 = make_double2(vr, vi);
       }
     }
   }
@@ -243,38 +267,23 @@ __global__ void __launch_bounds__(256, 2) k_interp_group(ConvArgs a) {
     // zero-weight nodes that pad a group to kGroupMax)
     for (int v = lane; v < kGroupMax * (NW / 4); v += 32) ((float4 *)wv)[v] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncwarp();
-    if (poly) {
-      // lane e: stencil point e % CUT of axis e / CUT for all nodes of the group
-      for (int e = lane; e < NV; e += 32) {
-        const int t = e / CUT, sidx = e - t * CUT;
+    // (node k, value e) pairs over the lanes; value e is stencil point e % CUT
+    // on axis e / CUT, stored at its offset in the union
+    for (int v = lane; v < g * NV; v += 32) {
+      const int k = v / NV, e = v - k * NV, t = e / CUT, sidx = e - t * CUT;
+      const float4 r = nd[k];
+      const float dist = t == 0 ? r.x : (t == 1 ? r.y : r.z);
+      const int sh = ((__float_as_int(r.w) >> (8 * t)) & 0xff) - (t == 0 ? x0 : (t == 1 ? y0 : z0));
+      float val;
+      if (poly && !(w.kind == WIN_BESSEL_I0 && sidx == 0 && dist == 0.f)) {
         const float4 *rw = (const float4 *)(s_poly + e * PS);
-        const float4 c0 = rw[0], c1 = rw[1], c2 = rw[2], c3 = rw[3];
-#pragma unroll
-        for (int k = 0; k < kGroupMax; k++) {
-          if (k < g) {
-            const float4 r = nd[k];
-            const float dist = t == 0 ? r.x : (t == 1 ? r.y : r.z);
-            const int sh = t == 0 ? ox[k] : (t == 1 ? oy[k] : oz[k]);
-            float v;
-            if (w.kind == WIN_BESSEL_I0 && sidx == 0 && dist == 0.f) window_point<float>(w, t, sidx, dist, 0, &v);
-            else v = poly_horner(c0, c1, c2, c3, dist - 0.5f);
-            wv[k * NW + t * 16 + sidx + sh] = v;
-          }
-        }
-      }
-    } else {
-      for (int v = lane; v < g * NV; v += 32) {
-        const int k = v / NV, e = v - k * NV, t = e / CUT, sidx = e - t * CUT;
-        const float4 r = nd[k];
-        const float dist = t == 0 ? r.x : (t == 1 ? r.y : r.z);
-        int sh = 0;
-#pragma unroll
-        for (int q = 0; q < kGroupMax; q++)
-          if (q == k) sh = t == 0 ? ox[q] : (t == 1 ? oy[q] : oz[q]);
+        val = poly_horner(rw[0], rw[1], rw[2], rw[3], dist - 0.5f);
+      } else {
         float out[3];
         window_point<float>(w, t, sidx, dist, 0, out);
-        wv[k * NW + t * 16 + sidx + sh] = out[0];
+        val = out[0];
       }
+      wv[k * NW + t * 16 + sidx + sh] = val;
     }
     __syncwarp();
     const int dx = x1 - x0, dy = y1 - y0, dz = z1 - z0;  // <= 1, 1, 3
