@@ -47,6 +47,10 @@ __device__ __forceinline__ void load_row(const double *p, double *v) {
 // elsewhere) is staged per node, so each update is a branch-free W-long FMA
 // run, and the node decode and the psi_x / psi_z loads serve both columns:
 //   acc[z] += f psi_x[a-o0] psi_y[b-o1] * psi_z[z-o2]
+// With f only (no gradient input) the node's rows are staged as f psi_x and
+// psi_y over the whole region (zero outside the node's stencil), so the
+// update of a thread has no coverage test at all; uncovered columns add
+// exact zeros.
 // When a node lies in a later slab the window slides: its first 4 values
 // are final for this CTA and are committed with vector atomics (zeros are
 // skipped).  Each z value of a column is therefore committed once per line
@@ -94,14 +98,21 @@ __device__ __forceinline__ void acc_fma(double2 &acc, double hr, double hi, doub
 }
 
 template <typename T, int CUT, int MODE>
-__global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1) k_spread_line(ConvArgs a) {
+__global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? ((MODE & 2) ? 4 : 5) : 1)
+    k_spread_line(ConvArgs a) {
   typedef typename Cplx<T>::type C;
   typedef LineGeom<CUT> G;
   constexpr int TL = G::TL, R = G::R, HR = G::HR, W = G::W, WP = G::WP, CP = G::CP, WREC = G::WREC;
   constexpr bool DF = (MODE & 1) != 0, DG = (MODE & 2) != 0;
   constexpr int NDER = DG ? 1 : 0;
   constexpr int NB = sizeof(T) == 4 ? 64 : 32;  // nodes per batch
-  constexpr int WSZ0 = (DG ? 2 : 1) * WREC;
+  // f only: [pz (WP)][f psi_x at region row a (R complex)][psi_y at region column b (R)],
+  // each part a multiple of 4 values so that every row stays 16-byte aligned
+  constexpr bool FONLY = !DG;
+  constexpr int R4 = (R + 3) / 4 * 4;
+  constexpr int WF = WP + 3 * R4;
+  static_assert(WP % 4 == 0 && WF % 4 == 0, "16-byte aligned node rows");
+  constexpr int WSZ0 = FONLY ? WF : 2 * WREC;
   constexpr int WSZ = (WSZ0 * sizeof(T) / 16) % 2 ? WSZ0 : WSZ0 + 16 / (int)sizeof(T);
   // per node: [pz (WP)][px (CP)][py (CP)] and, with DG, the same for the derivatives
   __shared__ __align__(16) T s_w[NB][WSZ];
@@ -175,10 +186,17 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
 #pragma unroll
       for (int c = 0; c < 8; c++) s_v[i][c] = v[c] * scale;
     }
-    for (int v = tid; v < nb * WP; v += nth) {
-      const int i = v / WP, z = v - i * WP;
-      s_w[i][z] = (T)0;
-      if (DG) s_w[i][WREC + z] = (T)0;
+    if (FONLY) {
+      for (int v = tid; v < nb * WF; v += nth) {
+        const int i = v / WF, z = v - i * WF;
+        s_w[i][z] = (T)0;
+      }
+    } else {
+      for (int v = tid; v < nb * WP; v += nth) {
+        const int i = v / WP, z = v - i * WP;
+        s_w[i][z] = (T)0;
+        s_w[i][WREC + z] = (T)0;
+      }
     }
     __syncthreads();
     // --- window values: all threads over (node, axis, stencil point) ------------
@@ -191,9 +209,23 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
       const int t = e / CUT, sidx = e - t * CUT;
       T out[3];
       window_point<T>(a.w, t, sidx, s_d[i][t], NDER, out);
-      const int pos = (t == 2) ? ((s_o[i] >> 16) & (TL - 1)) + sidx : WP + t * CP + sidx;
-      s_w[i][pos] = out[0];
-      if (DG) s_w[i][WREC + pos] = out[1];
+      if (FONLY) {
+        const int pk = s_o[i];
+        if (t == 2) {
+          s_w[i][((pk >> 16) & (TL - 1)) + sidx] = out[0];
+        } else if (t == 1) {
+          s_w[i][WP + 2 * R4 + ((pk >> 8) & 0xff) + sidx] = out[0];
+        } else {
+          // f psi_x, the product fr = psi_x f of the covered-column form
+          const int r = (pk & 0xff) + sidx;
+          s_w[i][WP + 2 * r] = out[0] * s_v[i][0];
+          s_w[i][WP + 2 * r + 1] = out[0] * s_v[i][1];
+        }
+      } else {
+        const int pos = (t == 2) ? ((s_o[i] >> 16) & (TL - 1)) + sidx : WP + t * CP + sidx;
+        s_w[i][pos] = out[0];
+        s_w[i][WREC + pos] = out[1];
+      }
     }
     __syncthreads();
     // --- accumulate, sliding the z window ----------------------------------------
@@ -235,6 +267,21 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? 5 : 1
         since = 0;
       }
       since++;
+      if (FONLY) {
+        const T *w = s_w[i];
+        const C zero2 = {(T)0, (T)0};
+        const C fa = active ? ((const C *)(w + WP))[ca] : zero2;
+        const T py0 = w[WP + 2 * R4 + cb], py1 = w[WP + 2 * R4 + cb + HR];
+        T pz[WP];
+        load_row<WP>(w, pz);
+        const T h0r = fa.x * py0, h0i = fa.y * py0, h1r = fa.x * py1, h1i = fa.y * py1;
+#pragma unroll
+        for (int z = 0; z < W; z++) {
+          acc_fma(acc[0][z], h0r, h0i, pz[z]);
+          acc_fma(acc[1][z], h1r, h1i, pz[z]);
+        }
+        continue;
+      }
       const int da = ca - (pk & 0xff), o1 = (pk >> 8) & 0xff;
       const bool row = active && (unsigned)da < (unsigned)CUT;
       const bool cov0 = row && (unsigned)(cb - o1) < (unsigned)CUT;
