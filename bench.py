@@ -260,7 +260,7 @@ def run_gpu(args):
     achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
     fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12
     roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": None, "kernel": {"interp": "k_interp_tile<float,13,1>",
+            "traffic": None, "kernel": {"interp": "k_interp_group<13>",
                                         "spread": "k_spread_line<float,13,1>"}[kname], "kernel_ms": kern_ms,
             "peak_source": peak_kind,
             "alg_bytes_per_launch": alg_bytes, "alg_flops_per_launch": alg_flops,
