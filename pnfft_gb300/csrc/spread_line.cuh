@@ -70,21 +70,27 @@ struct LineGeom {
 };
 constexpr int kFlushNodes = 256;
 
+// z mod n2 for 0 <= z (z < 2 n2 in all but the smallest grids: one subtraction)
+__device__ __forceinline__ int wrap_z(int z, int n2) {
+  if (z >= n2) z -= n2;
+  if (z >= n2) z %= n2;
+  return z;
+}
 // adds (r0 + i i0) at z and (r1 + i i1) at z+1 of one grid column (z even)
 __device__ __forceinline__ void commit_pair(float2 *col, int z, int n2, bool vec, float r0, float i0, float r1,
                                             float i1) {
   if (r0 == 0.f && i0 == 0.f && r1 == 0.f && i1 == 0.f) return;
   if (vec) {
-    atomicAdd((float4 *)(col + z % n2), make_float4(r0, i0, r1, i1));
+    atomicAdd((float4 *)(col + wrap_z(z, n2)), make_float4(r0, i0, r1, i1));
   } else {
-    if (r0 != 0.f || i0 != 0.f) atomicAdd(col + z % n2, make_float2(r0, i0));
-    if (r1 != 0.f || i1 != 0.f) atomicAdd(col + (z + 1) % n2, make_float2(r1, i1));
+    if (r0 != 0.f || i0 != 0.f) atomicAdd(col + wrap_z(z, n2), make_float2(r0, i0));
+    if (r1 != 0.f || i1 != 0.f) atomicAdd(col + wrap_z(z + 1, n2), make_float2(r1, i1));
   }
 }
 __device__ __forceinline__ void commit_pair(double2 *col, int z, int n2, bool, double r0, double i0, double r1,
                                             double i1) {
-  if (r0 != 0.0 || i0 != 0.0) atomic_add_grid(col + z % n2, make_double2(r0, i0));
-  if (r1 != 0.0 || i1 != 0.0) atomic_add_grid(col + (z + 1) % n2, make_double2(r1, i1));
+  if (r0 != 0.0 || i0 != 0.0) atomic_add_grid(col + wrap_z(z, n2), make_double2(r0, i0));
+  if (r1 != 0.0 || i1 != 0.0) atomic_add_grid(col + wrap_z(z + 1, n2), make_double2(r1, i1));
 }
 
 // acc += (hr + i hi) * p: the paired FMA of sm_100+ in FP32 (each component
@@ -202,7 +208,7 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? ((MOD
     // --- window values: all threads over (node, axis, stencil point) ------------
     // node-fastest (broadcast polynomial rows); the odd row stride in 16-byte
     // units keeps these stores to at most 4-way bank conflicts
-#pragma unroll 2  // two independent polynomial chains per thread
+#pragma unroll 4  // independent polynomial chains per thread
     for (int v = tid; v < NB * 3 * CUT; v += nth) {
       const int e = v / NB, i = v - e * NB;
       if (i >= nb) continue;
