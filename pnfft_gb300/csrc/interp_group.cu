@@ -1,8 +1,8 @@
 // interp_group.cu -- interpolation B of the FP32-mixed plans (f only) on a
 // group-mode binning: one warp per group of nodes with overlapping stencils.
 //
-// Reference: loop_over_particles_trafo (kernel/ndft-parallel.c:2703-2848)
-// with the stencil loop of kernel/assign.c:478-560, as in conv.cu.
+// Reference: loop_over_particles_trafo (kernel/ndft-parallel.c:2703-2888)
+// with the interpolation loops of kernel/assign.c:667-1159.
 #include <cuda_runtime.h>
 
 #include <atomic>

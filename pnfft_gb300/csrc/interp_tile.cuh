@@ -2,8 +2,8 @@
 // shared-memory copy of the tile's region; instantiated per precision in
 // interp_tile_f32.cu and interp_tile_f64.cu.
 //
-// Reference: loop_over_particles_trafo / _adj (kernel/ndft-parallel.c:2703-3009)
-// with the stencil loops of kernel/assign.c:478-1159.
+// Reference: loop_over_particles_trafo (kernel/ndft-parallel.c:2703-2888)
+// with the interpolation loops of kernel/assign.c:667-1159.
 #pragma once
 #include <cuda_runtime.h>
 

@@ -1,8 +1,8 @@
 // spread_line.cuh -- spreading B^T along lines of tiles; instantiated per
 // precision in spread_line_f32.cu and spread_line_f64.cu.
 //
-// Reference: loop_over_particles_trafo / _adj (kernel/ndft-parallel.c:2703-3009)
-// with the stencil loops of kernel/assign.c:478-1159.
+// Reference: loop_over_particles_adj (kernel/ndft-parallel.c:2890-3009) with
+// the spreading loops of kernel/assign.c:478-664.
 #pragma once
 #include <cuda_runtime.h>
 
