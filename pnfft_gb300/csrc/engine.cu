@@ -63,6 +63,7 @@ struct DevState {
   double *inv[3] = {nullptr, nullptr, nullptr};
   void *tab[3][3] = {{nullptr}};
   float *poly = nullptr;  // fitted FP32 window polynomials (nullptr: use the formula)
+  int poly_ncoef = kPolyCoef;  // coefficients used of each row (12 or 16)
   uint64_t tables_for = ~0ull;
   double *fhat = nullptr;
   size_t fhat_cap = 0;
@@ -182,35 +183,36 @@ static int window_kscale(pnfft_plan p, int t) {
   return (out[0] >= 2.0) ? (int)floor(log2(out[0])) : 0;
 }
 
-// Degree-15 fits of the window on each cell, for the FP32-mixed kernels.
+// Polynomial fits of the window on each cell, for the FP32-mixed kernels.
 // Every window is an entire function of y on each unit cell (Kaiser-Bessel
 // and Bessel-I0 through sinh(sqrt z)/sqrt z and I0(sqrt z) with z = b^2 (m^2 -
 // y^2), the B-spline a polynomial of degree 2m-1), so Chebyshev interpolation
-// at 16 points converges to FP64 round-off; the fit is converted to the
-// monomial basis in u = dist - 1/2 and rounded to float.  The fit is kept
-// only if, on 64 points per cell, it matches the FP64 formula to 1e-8 of the
-// largest value of each derivative order (else the kernels evaluate the
-// formula).  Derivatives come from the formula (psi', psi'' in x units).
-static bool fit_window_poly(pnfft_plan p, std::vector<float> &out) {
-  const int cut = p->cutoff, P = kPolyCoef - 1;
+// at ncoef points (degree ncoef - 1) converges fast; the fit is converted to
+// the monomial basis in u = dist - 1/2 and rounded to float, in rows of
+// kPolyCoef with zeros above ncoef.  The fit is kept only if, on 64 points
+// per cell, it matches the FP64 formula to 1e-8 of the largest value of each
+// derivative order (else the kernels evaluate the formula).  Derivatives
+// come from the formula (psi', psi'' in x units).
+static bool fit_window_poly(pnfft_plan p, std::vector<float> &out, int ncoef) {
+  const int cut = p->cutoff, P = ncoef - 1;
   out.assign((size_t)3 * 3 * cut * kPolyCoef, 0.f);
-  std::vector<double> f(kPolyCoef), c(kPolyCoef), mono(kPolyCoef), tkm1(kPolyCoef), tk(kPolyCoef), tn(kPolyCoef);
+  std::vector<double> f(ncoef), c(ncoef), mono(ncoef), tkm1(ncoef), tk(ncoef), tn(ncoef);
   for (int t = 0; t < 3; t++) {
     const double n = (double)p->n[t], b = p->b[t];
     const double sc = ldexp(1.0, -window_kscale(p, t));
     for (int der = 0; der <= 2; der++) {
       double vmax = 0.0, emax = 0.0;
       for (int s = 0; s < cut; s++) {
-        for (int j = 0; j < kPolyCoef; j++) {
-          const double d = 0.5 + 0.5 * cos(kPi * (j + 0.5) / kPolyCoef);
+        for (int j = 0; j < ncoef; j++) {
+          const double d = 0.5 + 0.5 * cos(kPi * (j + 0.5) / ncoef);
           double o[3];
           window_eval<double>(p->window, p->m, n, b, d + (double)(p->m - s), (double)s - d, der, o);
           f[j] = o[der];
         }
-        for (int k = 0; k < kPolyCoef; k++) {
+        for (int k = 0; k < ncoef; k++) {
           double sum = 0.0;
-          for (int j = 0; j < kPolyCoef; j++) sum += f[j] * cos(kPi * k * (j + 0.5) / kPolyCoef);
-          c[k] = 2.0 * sum / kPolyCoef;
+          for (int j = 0; j < ncoef; j++) sum += f[j] * cos(kPi * k * (j + 0.5) / ncoef);
+          c[k] = 2.0 * sum / ncoef;
         }
         c[0] *= 0.5;
         // sum_k c_k T_k(v), v = 2u, in monomials of v
@@ -222,13 +224,13 @@ static bool fit_window_poly(pnfft_plan p, std::vector<float> &out) {
         mono[0] = c[0];
         mono[1] = c[1];
         for (int k = 2; k <= P; k++) {
-          for (int i = 0; i < kPolyCoef; i++) tn[i] = (i > 0 ? 2.0 * tk[i - 1] : 0.0) - tkm1[i];
-          for (int i = 0; i < kPolyCoef; i++) mono[i] += c[k] * tn[i];
+          for (int i = 0; i < ncoef; i++) tn[i] = (i > 0 ? 2.0 * tk[i - 1] : 0.0) - tkm1[i];
+          for (int i = 0; i < ncoef; i++) mono[i] += c[k] * tn[i];
           tkm1 = tk;
           tk = tn;
         }
         float *row = &out[((size_t)(der * 3 + t) * cut + s) * kPolyCoef];
-        for (int i = 0; i < kPolyCoef; i++) {
+        for (int i = 0; i < ncoef; i++) {
           mono[i] *= ldexp(1.0, i) * sc;
           row[i] = (float)mono[i];
         }
@@ -280,11 +282,17 @@ static int ensure_tables(pnfft_plan p) {
     }
   if (d->poly) cudaFree(d->poly);
   d->poly = nullptr;
+  d->poly_ncoef = kPolyCoef;
   if (fp32(p) && p->intpol_order < 0) {
+    // the shortest fit that meets the tolerance: 12 coefficients, else 16
     std::vector<float> h;
-    if (fit_window_poly(p, h)) {
-      PG_CUDA(cudaMalloc(&d->poly, sizeof(float) * h.size()));
-      PG_CUDA(cudaMemcpy(d->poly, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice));
+    for (int nc : {12, kPolyCoef}) {
+      if (fit_window_poly(p, h, nc)) {
+        PG_CUDA(cudaMalloc(&d->poly, sizeof(float) * h.size()));
+        PG_CUDA(cudaMemcpy(d->poly, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice));
+        d->poly_ncoef = nc;
+        break;
+      }
     }
   }
   d->tables_for = want;
@@ -458,6 +466,7 @@ static WindowArgs window_args(pnfft_plan p) {
   for (int der = 0; der < 3; der++)
     for (int t = 0; t < 3; t++) w.tab[der][t] = p->dev->tab[der][t];
   w.poly = p->dev->poly;
+  w.poly_ncoef = p->dev->poly_ncoef;
   return w;
 }
 

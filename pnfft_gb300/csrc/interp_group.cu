@@ -277,7 +277,8 @@ __global__ void __launch_bounds__(256, 2) k_interp_group(ConvArgs a) {
       float val;
       if (poly && !(w.kind == WIN_BESSEL_I0 && sidx == 0 && dist == 0.f)) {
         const float4 *rw = (const float4 *)(s_poly + e * PS);
-        val = poly_horner(rw[0], rw[1], rw[2], rw[3], dist - 0.5f);
+        val = w.poly_ncoef <= 12 ? poly_horner12(rw[0], rw[1], rw[2], dist - 0.5f)
+                                 : poly_horner(rw[0], rw[1], rw[2], rw[3], dist - 0.5f);
       } else {
         float out[3];
         window_point<float>(w, t, sidx, dist, 0, out);

@@ -133,7 +133,7 @@ __device__ __forceinline__ void window_formula(const WindowArgs &w, int t, int s
   window_eval<double>(w.kind, w.m, (double)w.n[t], w.b[t], dist + (double)(w.m - s), (double)s - dist, nder, out);
 }
 
-// FP32: Horner on the fitted polynomial of stencil point s (16 FMAs per value)
+// FP32: Horner on the fitted polynomial of stencil point s (16 or 12 FMAs per value)
 __device__ __forceinline__ float poly_horner(const float4 &c0, const float4 &c1, const float4 &c2, const float4 &c3,
                                              float u) {
   float h = c3.w;
@@ -153,8 +153,25 @@ __device__ __forceinline__ float poly_horner(const float4 &c0, const float4 &c1,
   h = fmaf(h, u, c0.y);
   return fmaf(h, u, c0.x);
 }
-__device__ __forceinline__ float poly_eval(const float *row, float u) {
+// the same with the top four coefficients zero: Horner from a zero leading
+// term reaches c2.w exactly, so both give the same bits for such rows
+__device__ __forceinline__ float poly_horner12(const float4 &c0, const float4 &c1, const float4 &c2, float u) {
+  float h = c2.w;
+  h = fmaf(h, u, c2.z);
+  h = fmaf(h, u, c2.y);
+  h = fmaf(h, u, c2.x);
+  h = fmaf(h, u, c1.w);
+  h = fmaf(h, u, c1.z);
+  h = fmaf(h, u, c1.y);
+  h = fmaf(h, u, c1.x);
+  h = fmaf(h, u, c0.w);
+  h = fmaf(h, u, c0.z);
+  h = fmaf(h, u, c0.y);
+  return fmaf(h, u, c0.x);
+}
+__device__ __forceinline__ float poly_eval(const float *row, float u, int ncoef) {
   const float4 *r = (const float4 *)row;
+  if (ncoef <= 12) return poly_horner12(__ldg(r), __ldg(r + 1), __ldg(r + 2), u);
   return poly_horner(__ldg(r), __ldg(r + 1), __ldg(r + 2), __ldg(r + 3), u);
 }
 
@@ -167,7 +184,8 @@ __device__ __forceinline__ void window_point(const WindowArgs &w, int t, int s, 
     // the Bessel-I0 window jumps from 1/2 to 0 at y = m (s = 0, dist = 0)
     if (w.poly && w.intpol_order < 0 && !(w.kind == WIN_BESSEL_I0 && s == 0 && dist == 0.f)) {
       const float u = dist - 0.5f;
-      for (int d = 0; d <= nder; d++) out[d] = poly_eval(w.poly + ((d * 3 + t) * w.cut + s) * kPolyCoef, u);
+      for (int d = 0; d <= nder; d++)
+        out[d] = poly_eval(w.poly + ((d * 3 + t) * w.cut + s) * kPolyCoef, u, w.poly_ncoef);
       return;
     }
   }

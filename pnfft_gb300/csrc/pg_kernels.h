@@ -19,10 +19,12 @@ struct WindowArgs {
   int intpol_order;   // -1: evaluate directly; 0..3: tabulated (PNFFT_PRE_*_PSI)
   int intpol_K;       // samples per grid cell of the tables
   const void *tab[3][3];  // [derivative][axis], element type = compute precision
-  // FP32-mixed without PRE_*_PSI tables: per stencil point s a degree-15
-  // polynomial in u = dist - 1/2 for psi and its two derivatives, fitted on
-  // the host in FP64 (times 2^-kscale); layout [der][axis][s][16]
+  // FP32-mixed without PRE_*_PSI tables: per stencil point s a polynomial
+  // in u = dist - 1/2 for psi and its two derivatives, fitted on the host in
+  // FP64 (times 2^-kscale); layout [der][axis][s][16], poly_ncoef (12 or 16)
+  // coefficients used, the rest zero
   const float *poly;
+  int poly_ncoef;
 };
 constexpr int kPolyCoef = 16;
 
