@@ -60,6 +60,11 @@ int pnfft_gb300_set_stream(pnfft_plan ths, void *cuda_stream);
  * are the same bits; for timing).  Chosen per plan, e.g. by timing them. */
 int pnfft_gb300_set_conv_method(pnfft_plan ths, int method);
 int pnfft_gb300_get_conv_method(const pnfft_plan ths);
+/* The kernel family of the plan's last interpolation B (adjoint = 0) or
+ * spreading B^T (adjoint = 1): 0 none yet (or no nodes), 1 groups of nodes
+ * per warp (FP32-mixed B), 2 one warp per node over a tile, 3 lines of tiles
+ * (B^T), 4 one thread per node.  Set when the launch is issued. */
+int pnfft_gb300_get_conv_kernel(const pnfft_plan ths, int adjoint);
 
 /* Zero-copy mode.  When device arrays are attached, pnfft_trafo/pnfft_adj read
  * and write them directly and return without synchronizing the stream; the

@@ -239,8 +239,16 @@ class Plan:
         L.pnfft_gb300_set_device_f_hat(self._p, None)
 
     def set_conv_method(self, method):
-        """0: tiled interpolation / line-wise spreading (default); 1: one thread per node."""
+        """0: tiled interpolation / line-wise spreading (default); 1: one thread per node;
+        2: as 0 without node groups in the FP32-mixed interpolation."""
         _check(load().pnfft_gb300_set_conv_method(self._p, int(method)), "set_conv_method")
+
+    CONV_KERNELS = {0: "none", 1: "group", 2: "tile", 3: "line", 4: "generic"}
+
+    def conv_kernel(self, adjoint=False):
+        """Kernel family of the last B (or B^T with adjoint=True): "group",
+        "tile", "line", "generic" or "none"."""
+        return self.CONV_KERNELS.get(load().pnfft_gb300_get_conv_kernel(self._p, int(bool(adjoint))), "?")
 
     def trafo_device(self, x, f_hat, compute_flags=COMPUTE_F, f=None, grad=None, hess=None, stream=None,
                      fixed_nodes=False):

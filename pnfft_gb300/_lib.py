@@ -163,6 +163,7 @@ SIGNATURES = {
     "pnfft_gb300_set_stream": (_I, [_P, _P]),
     "pnfft_gb300_set_conv_method": (_I, [_P, _I]),
     "pnfft_gb300_get_conv_method": (_I, [_P]),
+    "pnfft_gb300_get_conv_kernel": (_I, [_P, _I]),
     "pnfft_gb300_set_device_f_hat": (_I, [_P, _P]),
     "pnfft_gb300_set_device_arrays": (_I, [_P, _P, _P, _P, _P]),
     "pnfft_gb300_nodes_set_fixed": (_I, [_P, _I]),

@@ -900,6 +900,9 @@ extern "C" int pnfft_gb300_set_conv_method(pnfft_plan ths, int method) {
   return 0;
 }
 extern "C" int pnfft_gb300_get_conv_method(const pnfft_plan ths) { return ths ? ths->conv_method : -1; }
+extern "C" int pnfft_gb300_get_conv_kernel(const pnfft_plan ths, int adjoint) {
+  return ths ? ths->last_conv[adjoint ? 1 : 0] : -1;
+}
 extern "C" int pnfft_gb300_set_stream(pnfft_plan ths, void *stream) { return ths ? engine_set_stream(ths, stream) : -1; }
 extern "C" int pnfft_gb300_set_device_f_hat(pnfft_plan ths, void *d) {
   if (!ths) return -1;

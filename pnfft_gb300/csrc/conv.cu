@@ -316,23 +316,25 @@ static bool tiles_usable(const ConvArgs &a) {
   return a.w.cut <= 15 && a.bin.T[0] == 8 && a.bin.T[1] == 8 && a.bin.T[2] == 8;
 }
 
-void launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s) {
-  if (a.M == 0) return;
-  bool done = false;
+int launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s) {
+  if (a.M == 0) return CONV_NONE;
   if (fp32 && mode == 1 && !a.generic && !a.no_group && a.bin.line_mode == BIN_GROUP && tiles_usable(a) &&
-      a.bin.sub_max <= kGroupSubMax)
-    done = launch_interp_group(a, s);
-  if (!done && !a.generic && a.bin.line_mode != BIN_LINE && tiles_usable(a))
-    done = fp32 ? launch_interp_tile_f32(a, mode, s) : launch_interp_tile_f64(a, mode, s);
-  if (!done) launch_interp_generic(a, mode, fp32, s);
+      a.bin.sub_max <= kGroupSubMax && launch_interp_group(a, s))
+    return CONV_GROUP;
+  if (!a.generic && a.bin.line_mode != BIN_LINE && tiles_usable(a) &&
+      (fp32 ? launch_interp_tile_f32(a, mode, s) : launch_interp_tile_f64(a, mode, s)))
+    return CONV_TILE;
+  launch_interp_generic(a, mode, fp32, s);
+  return CONV_GENERIC;
 }
 
-void launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s) {
-  if (a.M == 0) return;
-  bool done = false;
-  if (!a.generic && a.bin.line_mode == BIN_LINE && tiles_usable(a))
-    done = fp32 ? launch_spread_line_f32(a, mode, s) : launch_spread_line_f64(a, mode, s);
-  if (!done) launch_spread_generic(a, mode, fp32, s);
+int launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s) {
+  if (a.M == 0) return CONV_NONE;
+  if (!a.generic && a.bin.line_mode == BIN_LINE && tiles_usable(a) &&
+      (fp32 ? launch_spread_line_f32(a, mode, s) : launch_spread_line_f64(a, mode, s)))
+    return CONV_LINE;
+  launch_spread_generic(a, mode, fp32, s);
+  return CONV_GENERIC;
 }
 
 }  // namespace pg

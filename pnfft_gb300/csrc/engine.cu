@@ -743,10 +743,10 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
             c.stride = stride;
             if (mode & 4) {
               c.hess_out = out;
-              launch_interp(c, 4, f32, s);
+              p->last_conv[0] = launch_interp(c, 4, f32, s);
             } else if (mode == 1) {
               c.f_out = out;
-              launch_interp(c, 1, f32, s);
+              p->last_conv[0] = launch_interp(c, 1, f32, s);
             }
           }
           return 0;
@@ -782,8 +782,8 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
             c.grad_out = A.grad;
             c.hess_out = A.hess;
             int mode = ((cflags & C_F) ? 1 : 0) | ((cflags & C_GRAD) ? 2 : 0);
-            if (mode) launch_interp(c, mode, f32, s);
-            if (cflags & C_HESS) launch_interp(c, 4, f32, s);
+            if (mode) p->last_conv[0] = launch_interp(c, mode, f32, s);
+            if (cflags & C_HESS) p->last_conv[0] = launch_interp(c, 4, f32, s);
           }
         }
       }
@@ -899,7 +899,7 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
               c.stride = stride;
               c.f_in = fin;
               c.grad_in = gin;
-              launch_spread(c, mode, f32, s);
+              p->last_conv[1] = launch_spread(c, mode, f32, s);
             }
           }
           {

@@ -41,6 +41,7 @@ struct pnfft_plan_s {
   int precision;      // PNFFT_GB300_FP64 / PNFFT_GB300_FP32_MIXED
   int conv_method;    // 0: tiled/line kernels where usable, 1: one thread per node,
                       // 2: tiled without node groups in the FP32-mixed interpolation
+  int last_conv[2];   // pg::ConvKernel of the last B / B^T launch
   void *d_f_hat_user; // zero-copy f_hat
   void *user_stream;
   uint64_t uid;

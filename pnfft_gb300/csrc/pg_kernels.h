@@ -89,9 +89,11 @@ struct ConvArgs {
 
 // Launchers (conv.cu).  `fp32` selects the FP32-mixed kernels.  `mode` is a
 // bit set of 1 = f, 2 = grad, 4 = hessian (interp) / 1 = f, 2 = grad (spread).
+// launch_interp / launch_spread return the ConvKernel family they launched.
+enum ConvKernel { CONV_NONE = 0, CONV_GROUP = 1, CONV_TILE = 2, CONV_LINE = 3, CONV_GENERIC = 4 };
 void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s);
-void launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
-void launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
+int launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
+int launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
 // Kernel families behind launch_interp / launch_spread; each returns false
 // when it has no instance for the cutoff or mode.
 // FP32-mixed f-only interpolation on a BIN_GROUP binning (interp_group.cu)

@@ -110,28 +110,35 @@ def test_grouped_vs_oracle(gpu, oracle, win):
 
 
 def test_grouped_kernel_runs(gpu):
-    # the grouped kernel is the one launched for this workload (and not for
-    # method 2 or a gradient request)
-    torch = pytest.importorskip("torch")
-    from torch.profiler import ProfilerActivity, profile
-
+    # the kernel family each call launched (pnfft_gb300_get_conv_kernel): the
+    # grouped kernel for f on this workload, not for method 2, the gradient or
+    # the Hessian, nor with too few nodes per corner block; lines for B^T
     N = (16, 16, 16)
-    x = np.random.default_rng(5).uniform(-0.5, 0.5, (3000, 3))
+    rng = np.random.default_rng(5)
+    x = rng.uniform(-0.5, 0.5, (3000, 3))
+    f = rng.standard_normal(3000) + 1j * rng.standard_normal(3000)
 
-    def kernels(method, cflags):
+    def kernel(method, cflags, nodes=x, adjoint=False):
         p = gpu.Plan(N, m=6, precision="fp32")
         p.set_conv_method(method)
-        fh = spectrum(np.random.default_rng(1), p)
-        p.trafo(x, fh, cflags)  # binning and attributes outside the profile
-        with profile(activities=[ProfilerActivity.CUDA]) as prof:
-            p.trafo(x, fh, cflags)
-            torch.cuda.synchronize()
+        assert p.conv_kernel() == "none"
+        if adjoint:
+            p.adj(nodes, f[:nodes.shape[0]])
+        else:
+            p.trafo(nodes, spectrum(np.random.default_rng(1), p), cflags)
+        k = p.conv_kernel(adjoint)
         p.close()
-        return " ".join(e.name for e in prof.events())
+        return k
 
-    names = kernels(0, 1)
-    if "k_" not in names:
-        pytest.skip("the profiler recorded no kernels")
-    assert "k_interp_group" in names
-    assert "k_interp_group" not in kernels(2, 1)
-    assert "k_interp_group" not in kernels(0, 1 | 2)
+    assert kernel(0, gpu.COMPUTE_F) == "group"
+    assert kernel(2, gpu.COMPUTE_F) == "tile"
+    assert kernel(1, gpu.COMPUTE_F) == "generic"
+    assert kernel(0, gpu.COMPUTE_F | gpu.COMPUTE_GRAD_F) == "tile"
+    assert kernel(0, gpu.COMPUTE_HESSIAN_F) == "tile"
+    assert kernel(0, gpu.COMPUTE_F, nodes=x[:500]) == "tile"  # 500 nodes on 2048 corner blocks
+    assert kernel(0, gpu.COMPUTE_F, adjoint=True) == "line"
+    # FP64 plans interpolate one node per warp
+    p = gpu.Plan(N, m=6)
+    p.trafo(x, spectrum(np.random.default_rng(1), p))
+    assert p.conv_kernel() == "tile"
+    p.close()
