@@ -52,7 +52,7 @@ struct GroupGeom {
 // result of node k (output index jn of that lane)
 template <int CUT, int G>
 __device__ __forceinline__ void group_sums(const ConvArgs &a, const float2 *__restrict__ reg, const float *wv,
-                                           const int *ox, const int *oy, const int *oz, int x0, int y0, int z0,
+                                           const int *oy, const int *oz, int x0, int y0, int z0,
                                            int dx, int dy, int dz, int g, int lane, int jn, float scale) {
   typedef GroupGeom<CUT> Gm;
   constexpr int R = Gm::R, PL = Gm::PL, NW = Gm::NW;
@@ -240,14 +240,14 @@ __global__ void __launch_bounds__(256, 2) k_interp_group(ConvArgs a) {
     const int i0 = s_item[it], g = min(s_item[it + 1] - i0, kGroupMax);
     const float4 *nd = s_rec + i0;
     const int jn = lane < g ? s_perm[i0 + lane] : 0;
-    // corners: the union's lowest corner and each node's offset in it
-    int ox[kGroupMax], oy[kGroupMax], oz[kGroupMax];
+    // corners: the union's lowest corner and each node's offset in it (y, z;
+    // the x offset is in the window rows)
+    int oy[kGroupMax], oz[kGroupMax];
     int x0 = 255, y0 = 255, z0 = 255, x1 = 0, y1 = 0, z1 = 0;
 #pragma unroll
     for (int k = 0; k < kGroupMax; k++) {
       int o[3];
       unpack_corner(__float_as_int(nd[k < g ? k : 0].w), o);
-      ox[k] = o[0];
       oy[k] = o[1];
       oz[k] = o[2];
       x0 = min(x0, o[0]);
@@ -259,7 +259,6 @@ __global__ void __launch_bounds__(256, 2) k_interp_group(ConvArgs a) {
     }
 #pragma unroll
     for (int k = 0; k < kGroupMax; k++) {
-      ox[k] -= x0;
       oy[k] -= y0;
       oz[k] -= z0;
     }
@@ -290,7 +289,7 @@ __global__ void __launch_bounds__(256, 2) k_interp_group(ConvArgs a) {
     const int dx = x1 - x0, dy = y1 - y0, dz = z1 - z0;  // <= 1, 1, 3
     // one size of the sums keeps the hot code in the instruction cache;
     // smaller groups are padded with zero-weight nodes
-    group_sums<CUT, kGroupMax>(a, reg, wv, ox, oy, oz, x0, y0, z0, dx, dy, dz, g, lane, jn, scale);
+    group_sums<CUT, kGroupMax>(a, reg, wv, oy, oz, x0, y0, z0, dx, dy, dz, g, lane, jn, scale);
     __syncwarp();  // the group's slots are free
   }
 }
