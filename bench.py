@@ -32,6 +32,9 @@ CFG = dict(N=(128, 128, 128), n=(256, 256, 256), M=1 << 22, m=6)
 WORKLOAD = "c2c NFFT trafo+adj, N=128^3, n=256^3, M=2^22 uniform nodes, Kaiser-Bessel m=6"
 METRIC = "trafo+adj Mpts/s, N=128^3 M=2^22"
 L2_BYTES = 129 * 1024 * 1024
+# the kernels of B and B^T at the workload (FP32-mixed, cutoff 13)
+INTERP_KERNEL = "k_interp_group<13>"
+SPREAD_KERNEL = "k_spread_line<float,13,1>"
 
 
 def make_inputs(seed=2):
@@ -116,56 +119,76 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-def cpu_sample(nthreads=0, m_sample=1 << 15):
-    """Oracle (CPU port of the reference) on a bounded sample of the workload:
-    D/F/F^H/D^T on the full N=128^3 / n=256^3 grid and B/B^T on m_sample of
-    the nodes; the node-proportional part is scaled to M (M/m_sample)."""
+def cpu_threads():
+    """Host threads for the CPU legs: every core this process may use."""
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_step(inputs, nthreads):
+    """One step of the workload on the oracle, the CPU restatement of the
+    reference's FP64 path (OpenMP over nthreads, scipy FFT for PFFT): trafo =
+    D, F and B over all M nodes; adj = B^T over all M nodes, F^H and D^T.
+    Returns the step's seconds and the seconds of each stage, split like the
+    reference's timers (MATRIX_D, MATRIX_F, MATRIX_B of trafo and adj)."""
     from oracle import pnfft_oracle as O
-    x, fh, f = make_inputs()
+    x, fh, f = inputs
     N, n, M, m = CFG["N"], CFG["n"], CFG["M"], CFG["m"]
     p = O.OraclePlan(N, n, m=m, flags=0, nthreads=nthreads)
-    xs, fs = x[:m_sample].copy(), f[:m_sample].copy()
-    t0 = time.perf_counter()
-    g1 = p.trafo_D(fh, 0)
-    grid = p.forward_F(g1)
-    t1 = time.perf_counter()
-    out = np.zeros(m_sample, complex)
-    p.trafo_B(xs, grid, f=out.view(np.float64), cflags=O.COMPUTE_F)
-    t2 = time.perf_counter()
-    g = p.adjoint_B(xs, f=fs.view(np.float64), cflags=O.COMPUTE_F)
-    t3 = time.perf_counter()
-    gh = p.adjoint_F(g)
+    out = np.zeros(M, complex)
     acc = np.zeros(int(np.prod(p.local_N)), complex)
+    t = [time.perf_counter()]
+    g1 = p.trafo_D(fh, 0)
+    t.append(time.perf_counter())
+    grid = p.forward_F(g1)
+    t.append(time.perf_counter())
+    p.trafo_B(x, grid, f=out.view(np.float64), cflags=O.COMPUTE_F)
+    t.append(time.perf_counter())
+    g = p.adjoint_B(x, f=f.view(np.float64), cflags=O.COMPUTE_F)
+    t.append(time.perf_counter())
+    gh = p.adjoint_F(g)
+    t.append(time.perf_counter())
     p.adjoint_D(gh, 0, acc)
-    t4 = time.perf_counter()
-    fixed = (t1 - t0) + (t4 - t3)
-    per_node = ((t2 - t1) + (t3 - t2)) / m_sample
-    t_full = fixed + per_node * M
-    cores = nthreads if nthreads > 0 else O.num_threads()
-    return {"value": M / t_full / 1e6, "unit": "Mpts/s", "cores": cores, "kind": "port",
-            "sample": f"oracle FP64: D+F+F^H+D^T on the full 256^3 grid ({fixed:.2f} s) + B and B^T on "
-                      f"{m_sample} of the 2^22 nodes ({(t3 - t1):.2f} s), node part scaled by {M // m_sample}",
-            "seconds_per_step_extrapolated": t_full}
+    t.append(time.perf_counter())
+    stages = dict(zip(["trafo_D", "trafo_F", "trafo_B", "adj_B", "adj_F", "adj_D"], np.diff(t).tolist()))
+    return t[-1] - t[0], stages
+
+
+def cpu_baseline(steps=1, warmup=0, inputs=None):
+    """The oracle timed on the host cores over whole steps of the workload
+    (all M nodes, no sampling or scaling)."""
+    inputs = inputs if inputs is not None else make_inputs()
+    nt = cpu_threads()
+    for _ in range(warmup):
+        cpu_step(inputs, nt)
+    secs, stages = [], []
+    for _ in range(steps):
+        s, st = cpu_step(inputs, nt)
+        secs.append(s)
+        stages.append(st)
+    M = CFG["M"]
+    med = statistics.median(secs)
+    stage_med = {k: statistics.median(st[k] for st in stages) for k in stages[0]}
+    return {"value": M / med / 1e6, "unit": "Mpts/s", "cores": nt, "kind": "port",
+            "sample": f"oracle FP64 (C + OpenMP, scipy FFT): whole trafo+adj steps of the workload, all 2^22 nodes, "
+                      f"{steps} step(s), median {med:.2f} s",
+            "seconds_per_step": med, "stage_seconds": stage_med}, secs
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    for _ in range(args.warmup):
-        cpu_sample()
-    vals, secs = [], []
-    for _ in range(args.steps):
-        r = cpu_sample()
-        vals.append(r["value"])
-        secs.append(r["seconds_per_step_extrapolated"])
-    v = statistics.median(vals)
+    r, secs = cpu_baseline(steps=args.steps, warmup=args.warmup)
+    v = CFG["M"] * len(secs) / sum(secs) / 1e6
     line = {"metric": METRIC, "value": v, "unit": "Mpts/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * statistics.median(secs), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1e3 * sum(secs) / len(secs), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "precision": "fp64", "l2": "n/a (CPU)"}, "impl": "reference",
-            "cpu_baseline": {"value": v, "unit": "Mpts/s", "cores": r["cores"], "kind": "port",
-                             "sample": r["sample"]},
+            "cpu_baseline": {"value": v, "unit": "Mpts/s", "cores": r["cores"], "kind": r["kind"],
+                             "sample": r["sample"], "stage_seconds": r["stage_seconds"]},
             "e2e": {"value": v, "unit": "Mpts/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -250,23 +273,35 @@ def run_gpu(args):
     ms_tab, _, ftab, _ = device_steps(p32t, max(3, args.steps // 2), 2)
     p32t.close()
 
-    # --- dominant kernel roofline: interpolation B (trafo MATRIX_B) --------
+    # --- roofline of the dominant kernel (B or B^T, from the stage timers) --
+    # B and B^T do 2197 complex-by-real multiply-adds per node (5 flops with the
+    # weight), far above the HBM ridge: their roof is the FP32 FMA rate of the
+    # device, measured here with the paired FMA (FFMA2) the kernels use
+    L = P.load()
+    peak_ffma2, peak_ffma = ctypes.c_double(0), ctypes.c_double(0)
+    if L.pnfft_gb300_measure_fp32_fma(1, ctypes.byref(peak_ffma2)) or \
+            L.pnfft_gb300_measure_fp32_fma(0, ctypes.byref(peak_ffma)):
+        raise RuntimeError("FP32 FMA rate measurement failed: " + P.last_error())
     b_ms = statistics.mean(stage_b[0])
     bt_ms = statistics.mean(stage_b[1])
     kern_ms, kname = (b_ms, "interp") if b_ms >= bt_ms else (bt_ms, "spread")
     alg_bytes = M * (24 + 16) + int(np.prod(n)) * 8  # x (f64 x3) + f (c128) + grid (c64)
     alg_flops = M * (2 * m + 1) ** 3 * 5
     hbm, peak_kind = peaks()
-    achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
-    fp32_nominal = 152 * 128 * 2 * 2.07e9 / 1e12
-    roof = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": None, "kernel": {"interp": "k_interp_group<13>",
-                                        "spread": "k_spread_line<float,13,1>"}[kname], "kernel_ms": kern_ms,
-            "peak_source": peak_kind,
-            "alg_bytes_per_launch": alg_bytes, "alg_flops_per_launch": alg_flops,
-            "fp32_fma_tflops": alg_flops / (kern_ms * 1e-3) / 1e12,
-            "fp32_fma_frac_of_nominal": alg_flops / (kern_ms * 1e-3) / 1e12 / fp32_nominal,
-            "stage_ms": {"B": b_ms, "BT": bt_ms}}
+    tflops = lambda ms_: alg_flops / (ms_ * 1e-3) / 1e12  # noqa: E731
+    gbs = alg_bytes / (kern_ms * 1e-3) / 1e9
+    kernels = {"interp": INTERP_KERNEL, "spread": SPREAD_KERNEL}
+    roof = {"bound": "fp32", "achieved": tflops(kern_ms), "peak": peak_ffma2.value, "unit": "TFLOP/s",
+            "frac": tflops(kern_ms) / peak_ffma2.value, "traffic": None, "kernel": kernels[kname],
+            "kernel_ms": kern_ms,
+            "peak_source": "measured in this run: independent FFMA2 chains on every SM "
+                           "(pnfft_gb300_measure_fp32_fma), CUDA events",
+            "peak_scalar_ffma": peak_ffma.value,
+            "alg_flops_per_launch": alg_flops, "alg_bytes_per_launch": alg_bytes,
+            "stage_ms": {"B": b_ms, "BT": bt_ms},
+            "frac_by_kernel": {kernels["interp"]: tflops(b_ms) / peak_ffma2.value,
+                               kernels["spread"]: tflops(bt_ms) / peak_ffma2.value},
+            "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm, "peak_source": peak_kind}}
     traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic_file):
         try:
@@ -293,7 +328,6 @@ def run_gpu(args):
     pd.close()
 
     # --- e2e through the C ABI on page-locked host arrays -------------------
-    L = P.load()
     Nc = (ctypes.c_ssize_t * 3)(*N)
     nc = (ctypes.c_ssize_t * 3)(*n)
     xm = (ctypes.c_double * 3)(0.5, 0.5, 0.5)
@@ -381,7 +415,8 @@ def run_gpu(args):
         line["batched"] = run_batched(P, torch, dev)
         line["particles"] = run_particles(P, torch, dev)
     if rank == 0 and world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = {k: v for k, v in cpu_sample().items() if k != "seconds_per_step_extrapolated"}
+        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(inputs=(x, fh, f))[0].items()
+                                if k != "seconds_per_step"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -105,7 +105,9 @@ int pnfft_gb300_node_index(pnfft_plan ths, ptrdiff_t M, const double *x, int int
  *    most PNFFT_GB300_SORT_NOALLOC_MAX_NODES nodes (4.5 MiB); a larger M is
  *    refused with an error (-1).
  *  - The first call on a device resolves the array's address on that device
- *    (the device must be current); make it before any stream capture.
+ *    (the device must be current), and so does the first call after the
+ *    device's context was re-created (cudaDeviceReset); make that call before
+ *    any stream capture.
  *  - The work is queued on cuda_stream (NULL: the legacy default stream) and
  *    the call returns without synchronizing.
  *  - All calls share the array: calls whose work overlaps on the GPU race and
@@ -114,6 +116,14 @@ int pnfft_gb300_node_index(pnfft_plan ths, ptrdiff_t M, const double *x, int int
 #define PNFFT_GB300_SORT_NOALLOC_MAX_NODES 262144
 int pnfft_gb300_sort_nodes_noalloc(const pnfft_plan ths, ptrdiff_t M, const double *d_x, long long *d_pairs,
                                    void *cuda_stream);
+
+/* Measurement aid, no counterpart in the reference: the FP32 multiply-add
+ * rate of the current device in TFLOP/s (2 flops per multiply-add), timed with
+ * CUDA events over a kernel of independent FMA chains on every SM: scalar
+ * FFMA (paired = 0) or the paired FP32 FMA of sm_100+ (paired = 1), the
+ * instruction of the spreading and interpolation kernels.  Allocates 4 KiB of
+ * device memory for the result sink.  Returns 0 on success. */
+int pnfft_gb300_measure_fp32_fma(int paired, double *tflops);
 
 /* Milliseconds of the stages of the last pnfft_trafo / pnfft_adj of the plan,
  * indexed like the PNFFT_TIMER_* constants. */

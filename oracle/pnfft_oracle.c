@@ -15,8 +15,8 @@
  *     2679) is the same as this modulo wrap;
  *   - the F step itself (PFFT zero-pad + FFT, ndft-parallel.c:1524-1546) is done
  *     by the Python driver oracle/pnfft_oracle.py with scipy.fft.
- * Third-party arithmetic the reference takes from absent libraries is restated
- * from its published definition (see oracle/README.md):
+ * Third-party arithmetic the reference takes from libraries outside its tree
+ * is restated from its published definition:
  *   GSL gsl_sf_bessel_I0/I1 (kernel/bessel_i0.c:375, bessel_i1.c:570) -> power
  *   series; libcerf cerf() for PNFFT_WINDOW_GAUSSIAN_T (kernel/matrix_D.c:43)
  *   -> Re erf(a+iy) by quadrature of its defining integral.
@@ -657,11 +657,31 @@ void or_trafo_B(const or_plan *p, I64 M, const double *xall, const void *gridv, 
   const cplx *gc = (const cplx *)gridv;
   const double *gr = (const double *)gridv;
   const int need_d = (cflags & (C_GRAD | C_HESS)) != 0, need_dd = (cflags & C_HESS) != 0;
+  /* nodes are taken in the order of their lowest grid plane in axis 0 (as the
+   * reference's PNFFT_SORT_NODES does for cache reuse); every node's sum is
+   * independent of the order */
+  I64 *order = (I64 *)malloc(sizeof(I64) * (M > 0 ? M : 1));
+  {
+    I64 *cnt = (I64 *)calloc(n0 + 1, sizeof(I64));
+    I64 *pl = (I64 *)malloc(sizeof(I64) * (M > 0 ? M : 1));
+    for (I64 j = 0; j < M; j++) {
+      double x[3], fnx[3];
+      I64 u[3];
+      node_setup(p, xall + 3 * j, il, x, fnx, u);
+      pl[j] = wrapi(u[0], n0);
+      cnt[pl[j] + 1]++;
+    }
+    for (I64 q = 0; q < n0; q++) cnt[q + 1] += cnt[q];
+    for (I64 j = 0; j < M; j++) order[cnt[pl[j]]++] = j;
+    free(cnt);
+    free(pl);
+  }
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
-#pragma omp parallel for schedule(dynamic, 1024)
+#pragma omp parallel for schedule(dynamic, 256)
 #endif
-  for (I64 j = 0; j < M; j++) {
+  for (I64 q = 0; q < M; q++) {
+    const I64 j = order[q];
     double x[3], fnx[3], psi[3 * 64], dpsi[3 * 64], ddpsi[3 * 64];
     I64 u[3];
     node_setup(p, xall + 3 * j, il, x, fnx, u);
@@ -732,6 +752,7 @@ void or_trafo_B(const or_plan *p, I64 M, const double *xall, const void *gridv, 
         for (int c = 0; c < 6; c++) hc[6 * ind + c] += a_h[c];
     }
   }
+  free(order);
 }
 
 /* ---------------------------------------------------------------------------
@@ -805,11 +826,17 @@ static void spread_one(const or_plan *p, const double *xj, cplx fj, const cplx *
 
 void or_adjoint_B(const or_plan *p, I64 M, const double *xall, const double *f, const double *grad, I64 offset, I64 stride,
                   int use_il, int il, unsigned cflags, void *gridv, int nthreads) {
-  const I64 n0 = p->n[0];
+  const I64 n0 = p->n[0], n1 = p->n[1];
   const int cut = p->cutoff;
-  I64 nslab = n0 / cut;
-  if (nslab % 2) nslab--;
-  if (nthreads == 1 || nslab < 2) {
+  /* blocks of at least `cut` planes in axes 0 and 1; blocks of one colour
+   * (parities of both block indices) never touch the same grid points, so a
+   * colour's blocks run in parallel and the colours one after another */
+  I64 ns0 = n0 / cut, ns1 = n1 / cut;
+  if (ns0 % 2) ns0--;
+  if (ns1 % 2) ns1--;
+  if (ns1 < 2) ns1 = 1;
+  const I64 nblk = ns0 * ns1;
+  if (nthreads == 1 || ns0 < 2) {
     for (I64 j = 0; j < M; j++) {
       I64 ind = j * stride + offset;
       cplx fj = 0, gj[3] = {0, 0, 0};
@@ -826,32 +853,36 @@ void or_adjoint_B(const or_plan *p, I64 M, const double *xall, const double *f, 
     }
     return;
   }
-  /* bucket nodes by slab of their lowest x0 grid plane */
-  I64 *cnt = (I64 *)calloc(nslab + 1, sizeof(I64));
-  I64 *slab = (I64 *)malloc(sizeof(I64) * (M > 0 ? M : 1));
+  /* bucket nodes by the block of their lowest (x0, x1) grid planes */
+  I64 *cnt = (I64 *)calloc(nblk + 1, sizeof(I64));
+  I64 *blk = (I64 *)malloc(sizeof(I64) * (M > 0 ? M : 1));
   for (I64 j = 0; j < M; j++) {
     double x[3], fnx[3];
     I64 u[3];
     node_setup(p, xall + 3 * j, il, x, fnx, u);
-    I64 w = wrapi(u[0], n0);
-    I64 s = (w * nslab) / n0;
-    slab[j] = s;
-    cnt[s + 1]++;
+    I64 b0 = (wrapi(u[0], n0) * ns0) / n0;
+    I64 b1 = ns1 > 1 ? (wrapi(u[1], n1) * ns1) / n1 : 0;
+    blk[j] = b0 * ns1 + b1;
+    cnt[blk[j] + 1]++;
   }
-  for (I64 s = 0; s < nslab; s++) cnt[s + 1] += cnt[s];
-  I64 *pos = (I64 *)malloc(sizeof(I64) * (nslab + 1));
-  memcpy(pos, cnt, sizeof(I64) * (nslab + 1));
+  for (I64 b = 0; b < nblk; b++) cnt[b + 1] += cnt[b];
+  I64 *pos = (I64 *)malloc(sizeof(I64) * (nblk + 1));
+  memcpy(pos, cnt, sizeof(I64) * (nblk + 1));
   I64 *order = (I64 *)malloc(sizeof(I64) * (M > 0 ? M : 1));
-  for (I64 j = 0; j < M; j++) order[pos[slab[j]]++] = j;
+  for (I64 j = 0; j < M; j++) order[pos[blk[j]]++] = j;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
-  for (int parity = 0; parity < 2; parity++) {
+  const int ncol1 = ns1 > 1 ? 2 : 1;
+  for (int colour = 0; colour < 2 * ncol1; colour++) {
+    const I64 p0 = colour / ncol1, p1 = colour % ncol1;
+    const I64 h0 = (ns0 - p0 + 1) / 2, h1 = ns1 > 1 ? (ns1 - p1 + 1) / 2 : 1;
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 1)
 #endif
-    for (I64 s = parity; s < nslab; s += 2) {
-      for (I64 q = cnt[s]; q < cnt[s + 1]; q++) {
+    for (I64 t = 0; t < h0 * h1; t++) {
+      const I64 b = (p0 + 2 * (t / h1)) * ns1 + (ns1 > 1 ? p1 + 2 * (t % h1) : 0);
+      for (I64 q = cnt[b]; q < cnt[b + 1]; q++) {
         I64 j = order[q];
         I64 ind = j * stride + offset;
         cplx fj = 0, gj[3] = {0, 0, 0};
@@ -869,7 +900,7 @@ void or_adjoint_B(const or_plan *p, I64 M, const double *xall, const double *f, 
     }
   }
   free(cnt);
-  free(slab);
+  free(blk);
   free(pos);
   free(order);
 }
@@ -1266,6 +1297,74 @@ void or_init_f(I64 M, double *data) {
     data[2 * j + 1] = im;
   }
 }
+/* The adjoint NDFT of ndft-parallel.c:617-722 (f_hat[k] += f_j e^{+2 pi i k.x_j},
+ * c2c, f only) evaluated at the frequencies of a lattice k = (k0[i0], k1[i1],
+ * k2[i2]) instead of at all of them, summed over all M nodes.  Each node's
+ * factor is formed from one direct cexp per axis and frequency (no
+ * recurrence), so the FP64 values stay within a few ulps of the terms'.  Node
+ * chunks are summed by the threads in private lattices that are added in
+ * thread order.  out has n0*n1*n2 entries, i2 fastest. */
+void or_ndft_adj_lattice(I64 M, const double *x, const double *f, int n0, const I64 *k0, int n1, const I64 *k1,
+                         int n2, const I64 *k2, cplx *out, int nthreads) {
+  const I64 L = (I64)n0 * n1 * n2;
+  for (I64 i = 0; i < L; i++) out[i] = 0;
+  int nt = 1;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+  nt = omp_get_max_threads();
+#endif
+  double *acc = (double *)calloc((size_t)nt * 2 * L, sizeof(double));
+  if (!acc) return;
+#ifdef _OPENMP
+#pragma omp parallel
+#endif
+  {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    double *a = acc + (size_t)tid * 2 * L;
+    double *e = (double *)malloc(sizeof(double) * 2 * (size_t)(n0 + n1 + n2));
+    double *e0 = e, *e1 = e + 2 * n0, *e2 = e + 2 * (n0 + n1);
+#ifdef _OPENMP
+#pragma omp for schedule(static)
+#endif
+    for (I64 j = 0; j < M; j++) {
+      const double fr = f[2 * j], fi = f[2 * j + 1];
+      for (int i = 0; i < n0; i++) {
+        cplx v = cexp(+2.0 * PI * (double)k0[i] * x[3 * j] * I);
+        /* f_j e0 */
+        e0[2 * i] = fr * creal(v) - fi * cimag(v);
+        e0[2 * i + 1] = fr * cimag(v) + fi * creal(v);
+      }
+      for (int i = 0; i < n1; i++) {
+        cplx v = cexp(+2.0 * PI * (double)k1[i] * x[3 * j + 1] * I);
+        e1[2 * i] = creal(v);
+        e1[2 * i + 1] = cimag(v);
+      }
+      for (int i = 0; i < n2; i++) {
+        cplx v = cexp(+2.0 * PI * (double)k2[i] * x[3 * j + 2] * I);
+        e2[2 * i] = creal(v);
+        e2[2 * i + 1] = cimag(v);
+      }
+      double *o = a;
+      for (int i0 = 0; i0 < n0; i0++)
+        for (int i1 = 0; i1 < n1; i1++) {
+          const double br = e0[2 * i0] * e1[2 * i1] - e0[2 * i0 + 1] * e1[2 * i1 + 1];
+          const double bi = e0[2 * i0] * e1[2 * i1 + 1] + e0[2 * i0 + 1] * e1[2 * i1];
+          for (int i2 = 0; i2 < n2; i2++, o += 2) {
+            o[0] += br * e2[2 * i2] - bi * e2[2 * i2 + 1];
+            o[1] += br * e2[2 * i2 + 1] + bi * e2[2 * i2];
+          }
+        }
+    }
+    free(e);
+  }
+  for (int t = 0; t < nt; t++)
+    for (I64 i = 0; i < L; i++) out[i] += acc[(size_t)t * 2 * L + 2 * i] + acc[(size_t)t * 2 * L + 2 * i + 1] * I;
+  free(acc);
+}
+
 int or_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

@@ -101,6 +101,8 @@ def lib():
         L.or_ndft_adj.argtypes = [_VP, _I64P, _I64P, ctypes.c_int64, _DP, _DP, _DP, ctypes.c_uint, _VP,
                                   ctypes.c_int]
         L.or_sort_nodes.argtypes = [_VP, ctypes.c_int64, _DP, _I64P]
+        L.or_ndft_adj_lattice.argtypes = [ctypes.c_int64, _DP, _DP, ctypes.c_int, _I64P, ctypes.c_int, _I64P,
+                                          ctypes.c_int, _I64P, _VP, ctypes.c_int]
         L.or_srand.argtypes = [ctypes.c_uint]
         L.or_init_x_3d_adv.argtypes = [_DP, _DP, _DP, ctypes.c_int64, _DP]
         L.or_init_f.argtypes = [ctypes.c_int64, _DP]
@@ -247,7 +249,7 @@ class OraclePlan:
         grid = np.zeros(self.n, dtype=np.complex128)
         i0, i1, i2 = self._idx()
         grid[np.ix_(i0, i1, i2)] = cube
-        grid = scipy.fft.fftn(grid, workers=-1)
+        grid = scipy.fft.fftn(grid, workers=self.nthreads if self.nthreads > 0 else -1)
         if self.c2r:
             return np.ascontiguousarray(grid.real)
         return grid
@@ -255,7 +257,7 @@ class OraclePlan:
     def adjoint_F(self, grid):
         if self.c2r:
             grid = grid.astype(np.complex128)
-        full = scipy.fft.ifftn(grid, norm="forward", workers=-1)
+        full = scipy.fft.ifftn(grid, norm="forward", workers=self.nthreads if self.nthreads > 0 else -1)
         i0, i1, i2 = self._idx()
         return self._from_cube(full[np.ix_(i0, i1, i2)])
 
@@ -394,6 +396,19 @@ class OraclePlan:
             if not cflags & OMIT_DECONV:
                 self.adjoint_D(g1, il, f_hat)
         return f_hat
+
+
+def ndft_adj_lattice(x, f, k0, k1, k2, nthreads=0):
+    """FP64 adjoint NDFT (ndft-parallel.c:617-722, c2c, f only) at the
+    frequencies (k0[i0], k1[i1], k2[i2]) of a lattice, summed over all nodes;
+    returns a len(k0) x len(k1) x len(k2) complex array."""
+    x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
+    f = np.ascontiguousarray(f, dtype=np.complex128).reshape(-1)
+    ks = [np.ascontiguousarray(k, dtype=np.int64) for k in (k0, k1, k2)]
+    out = np.zeros((len(ks[0]), len(ks[1]), len(ks[2])), dtype=np.complex128)
+    lib().or_ndft_adj_lattice(x.shape[0], _p(x), _p(f.view(np.float64)), len(ks[0]), _p(ks[0], _I64P), len(ks[1]),
+                              _p(ks[1], _I64P), len(ks[2]), _p(ks[2], _I64P), _v(out), nthreads)
+    return out
 
 
 # --- reference input generators (glibc rand) --------------------------------

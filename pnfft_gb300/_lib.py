@@ -172,6 +172,7 @@ SIGNATURES = {
     "pnfft_gb300_node_index": (_I, [_P, _SS, _DP, _I, _LLP]),
     "pnfft_gb300_sort_nodes_noalloc": (_I, [_P, _SS, _P, _P, _P]),
     "pnfft_gb300_last_stage_ms": (_I, [_P, _I, _DP]),
+    "pnfft_gb300_measure_fp32_fma": (_I, [_I, _DP]),
 }
 
 _lib = None

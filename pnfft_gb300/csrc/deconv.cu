@@ -155,9 +155,21 @@ __global__ void k_deconv_crop_acc(DeconvArgs a) {
 
 static int row_threads(int64_t len) { return len >= 256 ? 256 : (len >= 128 ? 128 : 64); }
 
+// grid-stride passes: 64 resident blocks' worth per SM of the current device
+static int64_t max_blocks() {
+  static int sms[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152 * 64;
+  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 152 * 64;
+  }
+  return (int64_t)sms[dev] * 64;
+}
+
 void launch_deconv_pad(const DeconvArgs &a, bool fp32, cudaStream_t s) {
   const int64_t total = (int64_t)a.n[0] * a.n[1] * a.n[2];
-  const unsigned bl = (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, 152 * 64));
+  const unsigned bl = (unsigned)std::max<int64_t>(1, std::min<int64_t>((total + 255) / 256, max_blocks()));
   if (fp32) k_deconv_pad<float2><<<bl, 256, 0, s>>>(a);
   else k_deconv_pad<double2><<<bl, 256, 0, s>>>(a);
 }
@@ -167,7 +179,7 @@ void launch_deconv_crop_acc(const DeconvArgs &a, bool fp32, cudaStream_t s) {
   const int64_t rows = a.Nl[o0] * a.Nl[o1];
   if (rows <= 0 || a.Nl[o2] <= 0) return;
   const int th = row_threads(a.Nl[o2]);
-  const unsigned bl = (unsigned)std::min<int64_t>(rows, 152 * 64);
+  const unsigned bl = (unsigned)std::min<int64_t>(rows, max_blocks());
   if (fp32) k_deconv_crop_acc<float2><<<bl, th, 0, s>>>(a);
   else k_deconv_crop_acc<double2><<<bl, th, 0, s>>>(a);
 }

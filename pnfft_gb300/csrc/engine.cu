@@ -631,6 +631,26 @@ static int begin_call(pnfft_plan p, pnfft_nodes nd, const char *who) {
   return 0;
 }
 
+// Joins the auxiliary stream back into the plan's stream once it has been
+// forked, on every way out of a call: an error return must not leave the
+// upload of x or the binning running after the call (the caller may free or
+// reuse the arrays), nor leave an unjoined fork in a stream capture.
+struct ForkJoin {
+  DevState *d;
+  cudaStream_t s;
+  bool pending = false;
+  // the plan's stream waits for everything issued on the auxiliary stream so far
+  cudaError_t join() {
+    pending = false;
+    cudaError_t e = cudaEventRecord(d->ev_join, d->aux);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, d->ev_join, 0);
+    return e;
+  }
+  ~ForkJoin() {
+    if (pending) join();
+  }
+};
+
 // ---------------------------------------------------------------------------
 // pnfft_trafo
 // ---------------------------------------------------------------------------
@@ -648,9 +668,11 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
   // from the plan's stream, while D and F run; B waits for it
   const bool fork = nd && M > 0 && !(cflags & (PNFFT_OMIT_CONV | PNFFT_COMPUTE_DIRECT));
   cudaStream_t xs = fork ? d->aux : s;
+  ForkJoin fj{d, s};
   if (fork) {
     PG_CUDA(cudaEventRecord(d->ev_fork, s));
     PG_CUDA(cudaStreamWaitEvent(d->aux, d->ev_fork, 0));
+    fj.pending = true;
   }
   {
     StageScope whole(d, PNFFT_TIMER_WHOLE, 0);
@@ -669,7 +691,6 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
     if ((cflags & C_HESS) && M > 0 && !A.hess)
       return set_error("pnfft_trafo: missing memory allocation of nodes->hessian_f"), -1;
 
-    bool joined = !fork;
     if (cflags & PNFFT_COMPUTE_DIRECT) {
       NdftArgs na;
       memset(&na, 0, sizeof(na));
@@ -711,9 +732,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
           if (do_binning(p, nd, ca, ca.il, 0, d->aux)) return -1;
           pass_bin[pass] = ca.bin;
         }
-        PG_CUDA(cudaEventRecord(d->ev_join, d->aux));
       }
-      joined = !fork;
       for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
         const int il = il_plan ? pass : 0;
         ca.use_il = il_plan ? 1 : 0;
@@ -733,10 +752,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
             if (!(cflags & PNFFT_OMIT_FFT) && fft_exec(p, CUFFT_FORWARD)) return -1;
           }
           if (!(cflags & PNFFT_OMIT_CONV) && nd) {
-            if (!joined) {  // B needs the binning from the auxiliary stream
-              PG_CUDA(cudaStreamWaitEvent(s, d->ev_join, 0));
-              joined = true;
-            }
+            if (fj.pending) PG_CUDA(fj.join());  // B needs the binning from the auxiliary stream
             StageScope sc(d, PNFFT_TIMER_MATRIX_B, 0);
             ConvArgs c = ca;
             c.offset = off;
@@ -770,10 +786,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
             if (!(cflags & PNFFT_OMIT_FFT) && fft_exec(p, CUFFT_FORWARD)) return -1;
           }
           if (!(cflags & PNFFT_OMIT_CONV) && nd) {
-            if (!joined) {
-              PG_CUDA(cudaStreamWaitEvent(s, d->ev_join, 0));
-              joined = true;
-            }
+            if (fj.pending) PG_CUDA(fj.join());
             StageScope sc(d, PNFFT_TIMER_MATRIX_B, 0);
             ConvArgs c = ca;
             c.offset = 0;
@@ -788,7 +801,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
         }
       }
     }
-    if (!joined) PG_CUDA(cudaStreamWaitEvent(s, d->ev_join, 0));  // every path joins the fork
+    if (fj.pending) PG_CUDA(fj.join());  // every path joins the fork
     if (!zc && M > 0) {
       if (cflags & C_F) PG_CUDA(cudaMemcpyAsync(nd->f, A.f, sizeof(double) * tuple * M, cudaMemcpyDeviceToHost, s));
       if (cflags & C_GRAD)
@@ -822,11 +835,12 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
   // as in the trafo: the copy of x and the binning run on the auxiliary
   // stream while the plan's stream uploads f and clears f_hat and the grid
   const bool fork = nd && M > 0 && !(cflags & (PNFFT_OMIT_CONV | PNFFT_COMPUTE_DIRECT));
+  ForkJoin fj{d, s};
   if (fork) {
     PG_CUDA(cudaEventRecord(d->ev_fork, s));
     PG_CUDA(cudaStreamWaitEvent(d->aux, d->ev_fork, 0));
+    fj.pending = true;
   }
-  bool joined = !fork;
   {
     StageScope whole(d, PNFFT_TIMER_WHOLE, 1);
     if (resolve_arrays(p, nd, cflags, true, A, zc, fork ? d->aux : s)) return -1;
@@ -876,7 +890,6 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
           if (do_binning(p, nd, ca, ca.il, 1, d->aux)) return -1;
           pass_bin[pass] = ca.bin;
         }
-        PG_CUDA(cudaEventRecord(d->ev_join, d->aux));
       }
       for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
         const int il = il_plan ? pass : 0;
@@ -887,10 +900,7 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
         auto one = [&](int ikmode, int ikdim, const double *fin, const double *gin, int64_t off, int64_t stride,
                        int mode) -> int {
           PG_CUDA(cudaMemsetAsync(d->grid, 0, gbytes, s));
-          if (!joined) {  // B^T needs the binning from the auxiliary stream
-            PG_CUDA(cudaStreamWaitEvent(s, d->ev_join, 0));
-            joined = true;
-          }
+          if (fj.pending) PG_CUDA(fj.join());  // B^T needs the binning from the auxiliary stream
           {
             StageScope sc(d, PNFFT_TIMER_MATRIX_B, 1);
             if (!(cflags & PNFFT_OMIT_CONV) && nd) {
@@ -925,7 +935,7 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
         }
       }
     }
-    if (!joined) PG_CUDA(cudaStreamWaitEvent(s, d->ev_join, 0));  // every path joins the fork
+    if (fj.pending) PG_CUDA(fj.join());  // every path joins the fork
     if (!p->d_f_hat_user && fb > 0) {
       if (!p->f_hat) return set_error("pnfft_adj: f_hat is not allocated"), -1;
       PG_CUDA(cudaMemcpyAsync(p->f_hat, A.fhat, fb, cudaMemcpyDeviceToHost, s));

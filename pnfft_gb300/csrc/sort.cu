@@ -9,6 +9,7 @@
 // histograms, a digit-major scan over blocks, and an in-order scatter in which
 // a warp ranks equal digits with __match_any_sync), so the permutation is
 // identical to the reference's.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -186,10 +187,13 @@ int radix_sort_nodes(const double *x, int64_t M, const int *n, int m, long long 
 // the per-block digit histograms -- from one statically sized device array
 // instead of cudaMallocAsync.  The array is part of this module's device
 // image and exists once per device; its address is resolved with
-// cudaGetSymbolAddress on the first call made on each device (with that
-// device current), so make one call on a device before any stream capture on
-// it.  The array holds at most kNoAllocMaxNodes nodes; larger calls are
-// refused with an error and must use the allocating sort.
+// cudaGetSymbolAddress by the first call made in each CUDA context (with that
+// context's device current): once per device, and once more after the
+// context has been destroyed and re-created (cudaDeviceReset), since a new
+// context loads the module at another address.  That first call may load the
+// module, so make it before any stream capture in the context.  The array
+// holds at most kNoAllocMaxNodes nodes; larger calls are refused with an
+// error and must use the allocating sort.
 //
 // Every call shares the array and finds the previous call's contents in it.
 // Nothing there has to start at zero: every radix pass writes each digit
@@ -209,21 +213,51 @@ static_assert(kNoAllocPairBytes % 256 == 0, "histograms start 256-byte aligned")
 
 constexpr int kNoAllocMaxDevices = 64;
 static std::mutex g_scratch_mu;
+// per device: the scratch address and the unique ID of the context it was resolved in
 static void *g_scratch_ptr[kNoAllocMaxDevices] = {};
+static unsigned long long g_scratch_ctx[kNoAllocMaxDevices] = {};
+
+// the unique ID of the current context (cuCtxGetId, CUDA 12.0+, reached
+// through the runtime's driver entry points so that no libcuda link is needed)
+static int current_context_id(unsigned long long *id) {
+  typedef CUresult (*get_current_t)(CUcontext *);
+  typedef CUresult (*get_id_t)(CUcontext, unsigned long long *);
+  static get_current_t get_current = nullptr;
+  static get_id_t get_id = nullptr;
+  if (!get_current || !get_id) {
+    void *f0 = nullptr, *f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+      return -1;
+    get_current = (get_current_t)f0;
+    get_id = (get_id_t)f1;
+  }
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, id) != CUDA_SUCCESS) return -1;
+  return 0;
+}
 
 static int sort_scratch_address(void **out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaSetDevice(dev);  // initialises the primary context and makes it current
   if (e != cudaSuccess) {
-    set_error("pnfft_gb300_sort_nodes_noalloc: cudaGetDevice failed: %s", cudaGetErrorString(e));
+    set_error("pnfft_gb300_sort_nodes_noalloc: no usable CUDA device: %s", cudaGetErrorString(e));
     return -1;
   }
   if (dev < 0 || dev >= kNoAllocMaxDevices) {
     set_error("pnfft_gb300_sort_nodes_noalloc: device %d is beyond the %d devices supported", dev, kNoAllocMaxDevices);
     return -1;
   }
+  unsigned long long ctx = 0;
+  if (current_context_id(&ctx)) {
+    set_error("pnfft_gb300_sort_nodes_noalloc: the current CUDA context of device %d could not be identified", dev);
+    return -1;
+  }
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_ptr[dev]) {
+  if (!g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
     void *ptr = nullptr;
     e = cudaGetSymbolAddress(&ptr, g_sort_scratch);
     if (e != cudaSuccess || !ptr) {
@@ -232,6 +266,7 @@ static int sort_scratch_address(void **out) {
       return -1;
     }
     g_scratch_ptr[dev] = ptr;
+    g_scratch_ctx[dev] = ctx;
   }
   *out = g_scratch_ptr[dev];
   return 0;

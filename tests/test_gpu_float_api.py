@@ -56,9 +56,9 @@ def test_float_api_trafo_adj(lib, oracle, c2r):
     x64 = x.astype(np.float64)
     wf, wg, _ = o.trafo(x64, fh.astype(np.complex128), lib.COMPUTE_F | lib.COMPUTE_GRAD_F)
     if c2r:
-        assert _rel(f, wf) < 3e-6 and _rel(g, wg.ravel()) < 3e-6
+        assert _rel(f, wf) < 1e-6 and _rel(g, wg.ravel()) < 1e-6
     else:
-        assert _rel(f.view(np.complex64), wf) < 3e-6 and _rel(g.view(np.complex64), wg.ravel()) < 3e-6
+        assert _rel(f.view(np.complex64), wf) < 1e-6 and _rel(g.view(np.complex64), wg.ravel()) < 1e-6
     # accumulated trafo adds to the float outputs
     L.pnfftf_trafo(p, nd, lib.COMPUTE_F | lib.COMPUTE_ACCUMULATED)
     f2 = _view(L.pnfftf_get_f(nd), tu * M).copy()
@@ -70,6 +70,6 @@ def test_float_api_trafo_adj(lib, oracle, c2r):
     L.pnfftf_adj(p, nd, lib.COMPUTE_F)
     a = _view(L.pnfftf_get_f_hat(p), 2 * nfh).copy().view(np.complex64)
     wa = o.adj(x64, fv.astype(np.float64 if c2r else np.complex128))
-    assert _rel(a, wa) < 3e-6
+    assert _rel(a, wa) < 1e-6
     L.pnfftf_free_nodes(nd, lib.FREE_X | lib.FREE_F | lib.FREE_GRAD_F)
     L.pnfftf_finalize(p, lib.FREE_F_HAT)

@@ -106,7 +106,7 @@ def test_grouped_vs_oracle(gpu, oracle, win):
     p = gpu.Plan(N, m=6, flags=WINDOWS[win], precision="fp32")
     o = oracle.OraclePlan(N, m=6, flags=WINDOWS[win])
     fh = spectrum(rng, p)
-    assert rel(p.trafo(x, fh)[0], o.trafo(x, fh)[0]) < 2e-6
+    assert rel(p.trafo(x, fh)[0], o.trafo(x, fh)[0]) < 1e-6
 
 
 def test_grouped_kernel_runs(gpu):

@@ -3,7 +3,9 @@
 FP64: every transform variant agrees with the oracle's restatement of the
 reference on the same inputs to 1e-12 relative l2 (spec bar); node
 indices and the PNFFT_SORT_NODES permutation are bit-exact.
-FP32-mixed: within 2e-6 relative l2 of the FP64 NDFT at m = 6.
+FP32-mixed: within 1e-6 relative l2 of the FP64 NDFT at m = 6 (FP32_TOL, the
+bar of the FP32-mixed form for f, grad_f and the adjoint); Hessians, which
+are outside that bar, within 5e-6 of the FP64 oracle.
 """
 import numpy as np
 import pytest
@@ -19,6 +21,7 @@ WINDOWS = {
     "gaussian_t": (1 << 17) | (1 << 13),
 }
 FP64_TOL = 1e-12
+FP32_TOL = 1e-6
 
 
 def rel(a, b):
@@ -110,7 +113,7 @@ def test_odd_and_wrapping_grids(gpu, oracle, n, m):
     o = oracle.OraclePlan(N, n, m=m)
     want_t = o.trafo(x, fh, 1 | 2)
     want_a = o.adj(x, f, g, 1 | 2)
-    for prec, tol in (("fp64", FP64_TOL), ("fp32", 3e-6)):
+    for prec, tol in (("fp64", FP64_TOL), ("fp32", FP32_TOL)):
         p = gpu.Plan(N, n, m=m, precision=prec)
         got_t = p.trafo(x, fh, 1 | 2)
         assert rel(got_t[0], want_t[0]) < tol and rel(got_t[1], want_t[1]) < tol, prec
@@ -207,12 +210,12 @@ def test_fp32_mixed_vs_ndft(gpu, oracle):
     sub = slice(0, 512)
     f, g, _ = p.trafo(x, fh, 1 | 2)
     fd, gd, _ = o.trafo(x[sub], fh, 1 | 2 | gpu.COMPUTE_DIRECT)
-    assert rel(f[sub], fd) < 2e-6
-    assert rel(g[sub], gd) < 2e-6
+    assert rel(f[sub], fd) < FP32_TOL
+    assert rel(g[sub], gd) < FP32_TOL
     fv = rng.standard_normal(M) + 1j * rng.standard_normal(M)
     a = p.adj(x, fv)
     ad = o.adj(x, fv, None, 1 | gpu.COMPUTE_DIRECT)
-    assert rel(a, ad) < 2e-6
+    assert rel(a, ad) < FP32_TOL
 
 
 def test_fp32_tiny_and_edge_coordinates(gpu, oracle):
@@ -230,8 +233,8 @@ def test_fp32_tiny_and_edge_coordinates(gpu, oracle):
     p = gpu.Plan(N, m=6, precision="fp32")
     o = oracle.OraclePlan(N, m=6)
     got, want = p.trafo(x, fh)[0], o.trafo(x, fh)[0]
-    assert np.abs(got - want).max() <= 2e-6 * np.abs(want).max()
-    assert rel(p.adj(x, f), o.adj(x, f)) < 2e-6
+    assert np.abs(got - want).max() <= FP32_TOL * np.abs(want).max()
+    assert rel(p.adj(x, f), o.adj(x, f)) < FP32_TOL
 
 
 @pytest.mark.parametrize("win", list(WINDOWS))
@@ -244,9 +247,9 @@ def test_fp32_mixed_all_windows_vs_fp64_oracle(gpu, oracle, win):
     o = oracle.OraclePlan(N, m=6, flags=WINDOWS[win])
     got = p.trafo(x, fh, CF_ALL)
     want = o.trafo(x, fh, CF_ALL)
-    for a, b, tol in zip(got, want, (2e-6, 2e-6, 5e-6)):
+    for a, b, tol in zip(got, want, (FP32_TOL, FP32_TOL, 5e-6)):
         assert rel(a, b) < tol, (win, rel(a, b))
-    assert rel(p.adj(x, f, g, 1 | 2), o.adj(x, f, g, 1 | 2)) < 2e-6
+    assert rel(p.adj(x, f, g, 1 | 2), o.adj(x, f, g, 1 | 2)) < FP32_TOL
 
 
 def test_accumulated_and_empty(gpu, oracle):
@@ -276,7 +279,7 @@ def test_clustered_nodes_large_bins(gpu, oracle):
     x = np.concatenate([rng.uniform(-0.5, 0.5, (500, 3)), 0.2 + 0.002 * rng.standard_normal((5000, 3))])
     fh = rng.standard_normal(4096) + 1j * rng.standard_normal(4096)
     f = rng.standard_normal(x.shape[0]) + 0j
-    for prec, tol in (("fp64", FP64_TOL), ("fp32", 2e-6)):
+    for prec, tol in (("fp64", FP64_TOL), ("fp32", FP32_TOL)):
         p = gpu.Plan(N, m=5, precision=prec)
         o = oracle.OraclePlan(N, m=5)
         assert rel(p.trafo(x, fh)[0], o.trafo(x, fh)[0]) < tol
@@ -315,12 +318,12 @@ def test_fixed_nodes_reuse_device_coordinates(gpu, oracle):
     a1 = p.trafo(x, fh)[0].copy()
     a2 = p.trafo(x, fh)[0].copy()
     np.testing.assert_array_equal(a1, a2)
-    assert rel(a1, o.trafo(x, fh)[0]) < 3e-6
+    assert rel(a1, o.trafo(x, fh)[0]) < FP32_TOL
     x2 = np.ascontiguousarray(np.roll(x, 1, axis=0))  # another array: pnfft_set_x sees a new pointer
     b = p.trafo(x2, fh)[0]
-    assert rel(b, o.trafo(x2, fh)[0]) < 3e-6
+    assert rel(b, o.trafo(x2, fh)[0]) < FP32_TOL
     L.pnfft_gb300_nodes_set_fixed(nd, 0)
-    assert rel(p.adj(x, f), o.adj(x, f)) < 3e-6
+    assert rel(p.adj(x, f), o.adj(x, f)) < FP32_TOL
 
 
 @pytest.mark.parametrize("flags", ["interlaced", "diff_ik", "interlaced_ik", "transposed_interlaced"])
@@ -328,7 +331,7 @@ def test_c2r_mode_combinations(gpu, oracle, flags):
     fl = {"interlaced": gpu.INTERLACED, "diff_ik": gpu.DIFF_IK, "interlaced_ik": gpu.INTERLACED | gpu.DIFF_IK,
           "transposed_interlaced": gpu.TRANSPOSED_F_HAT | gpu.INTERLACED}[flags]
     N = (12, 8, 16)
-    for prec, tol in (("fp64", FP64_TOL), ("fp32", 3e-6)):
+    for prec, tol in (("fp64", FP64_TOL), ("fp32", FP32_TOL)):
         p = gpu.Plan(N, m=4, flags=fl, c2r=True, precision=prec)
         o = oracle.OraclePlan(N, m=4, flags=fl, c2r=True)
         x, fh, f, g = case(N, 600, 18, c2r=True, local_N=p.local_N)

@@ -2,7 +2,9 @@
 device array instead of device allocations.  Called through the C ABI on
 device arrays and compared with the allocating pnfft_gb300_sort_nodes on two
 calls in a row (the second finds the first call's contents in the shared
-scratch), at the size limit, and for sizes the entry point must refuse.
+scratch), at the size limit, and for sizes the entry point must refuse.  At
+the size limit it is also compared with the oracle's CPU restatement of the
+reference sort, so that a fault shared by both device sorts cannot pass.
 This file is collected last on purpose: it must pass alone in a fresh process
 and after every other test."""
 import ctypes
@@ -18,7 +20,7 @@ def _noalloc(L, plan, dx, dpairs, M):
                                             ctypes.c_void_p(dpairs.data_ptr()), None)
 
 
-def test_sort_noalloc_matches_allocating_sort(lib):
+def test_sort_noalloc_matches_allocating_sort(lib, oracle):
     torch = pytest.importorskip("torch")
     if lib.device_count() == 0:
         pytest.fail("no CUDA device visible for a -m gpu test")
@@ -43,6 +45,10 @@ def test_sort_noalloc_matches_allocating_sort(lib):
         got = dpairs.cpu().numpy().reshape(-1, 2)
         want = plan.sort_nodes(x)
         np.testing.assert_array_equal(got, want)
+        if M == MAX:
+            # the same plan on the CPU: sort_nodes_for_better_cache_handle restated
+            o = oracle.OraclePlan((32, 48, 64), m=5)
+            np.testing.assert_array_equal(got, o.sort_nodes(x))
     # a plan with an odd number of radix passes ends in the scratch buffer
     small = lib.Plan((8, 8, 8), m=2)  # n = 16^3: 12 key bits, two passes
     odd = lib.Plan((64, 64, 64), m=3)  # n = 128^3: 21 key bits, three passes
