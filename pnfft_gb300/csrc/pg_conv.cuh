@@ -190,8 +190,10 @@ __device__ __forceinline__ void window_point(const WindowArgs &w, int t, int s, 
     }
   }
   if (w.intpol_order >= 0) {
+    // an FP32 fraction can round up to exactly 1 (FP64 ones stay below 1):
+    // the last sub-interval, evaluated at its right end, gives the window there
     T dK = dist * (T)w.intpol_K;
-    int k = (int)floor(dK);
+    int k = min((int)floor(dK), w.intpol_K - 1);
     T dk = dK - (T)k;
     size_t base = ((size_t)k * w.cut + s) * (size_t)(w.intpol_order + 1);
     for (int d = 0; d <= nder; d++) out[d] = intpol<T>(w.intpol_order, (const T *)w.tab[d][t] + base, dk);

@@ -74,8 +74,11 @@ def test_config1_fp64_vs_oracle_nfft_and_ndft(gpu, oracle):
     assert e_gpu < 1e-6 and abs(e_gpu - e_or) <= 1e-9 * e_or
     e_gpu, e_or = rel(fa, ad), rel(ao, ad)
     assert e_gpu < 1e-6 and abs(e_gpu - e_or) <= 1e-9 * e_or
-    # the check_trafo.c / check_adj.c error figure: max |f - f_direct| / sum |f_hat|
-    assert np.abs(ft - fd).max() / np.abs(fh).sum() < 1e-9
+    # the error figure check_trafo.c prints, max |f - f_direct| / sum |f_hat|,
+    # is the oracle's (the window's aliasing error at m = 4)
+    e_gpu = np.abs(ft - fd).max() / np.abs(fh).sum()
+    e_or = np.abs(fo - fd).max() / np.abs(fh).sum()
+    assert e_gpu < 1e-8 and abs(e_gpu - e_or) <= 1e-6 * e_or
 
 
 def test_config1_fp32_mixed_vs_ndft(gpu, oracle):
@@ -124,8 +127,10 @@ def test_config2_fp64_trafo_with_gradient_vs_oracle(gpu, cfg2):
     fo, go, _ = c["o"].trafo(c["xs"], c["fh"], CF_FG)
     assert rel(f[:SUB], fo) < FP64_TOL
     assert rel(g[:SUB], go) < FP64_TOL
-    # and the window error of the FP64 path against the direct NDFT
-    assert rel(f[:SUB], c["fd"]) < 1e-10 and rel(g[:SUB], c["gd"]) < 1e-10
+    # the window's aliasing error against the direct NDFT is the oracle's
+    for got, want, nd in ((f[:SUB], fo, c["fd"]), (g[:SUB], go, c["gd"])):
+        e_gpu, e_or = rel(got, nd), rel(want, nd)
+        assert e_gpu < 1e-8 and abs(e_gpu - e_or) <= 1e-3 * e_or
 
 
 def test_config2_fp64_adj_vs_oracle(gpu, cfg2):
