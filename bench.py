@@ -33,7 +33,7 @@ WORKLOAD = "c2c NFFT trafo+adj, N=128^3, n=256^3, M=2^22 uniform nodes, Kaiser-B
 METRIC = "trafo+adj Mpts/s, N=128^3 M=2^22"
 L2_BYTES = 129 * 1024 * 1024
 # the kernels of B and B^T at the workload (FP32-mixed, cutoff 13)
-INTERP_KERNEL = "k_interp_group<13>"
+INTERP_KERNEL = "k_interp_line<13>"
 SPREAD_KERNEL = "k_spread_line<float,13,1>"
 
 

@@ -53,17 +53,20 @@ int pnfft_gb300_get_precision(const pnfft_plan ths);
  * stream is capturing.  Host arrays are refused during capture. */
 int pnfft_gb300_set_stream(pnfft_plan ths, void *cuda_stream);
 
-/* Convolution kernels of a plan: 0 = tiled B and line-wise B^T where the
- * cutoff and grid allow (default), 1 = one thread per node (small node
- * counts on large grids), 2 = as 0 but the FP32-mixed B takes one node per
- * warp instead of groups of nodes with overlapping stencils (the results
- * are the same bits; for timing).  Chosen per plan, e.g. by timing them. */
+/* Convolution kernels of a plan, chosen per plan (e.g. by timing them):
+ *  0 = default: B^T along lines of tiles; the FP32-mixed B of f alone along
+ *      the same lines, other B one warp per node over a tile (cutoff and
+ *      grid permitting);
+ *  1 = one thread per node (small node counts on large grids);
+ *  2 = B one warp per node over a tile also for the FP32-mixed f;
+ *  3 = the FP32-mixed B of f in groups of nodes with overlapping stencils
+ *      per warp (the same bits as 2). */
 int pnfft_gb300_set_conv_method(pnfft_plan ths, int method);
 int pnfft_gb300_get_conv_method(const pnfft_plan ths);
 /* The kernel family of the plan's last interpolation B (adjoint = 0) or
  * spreading B^T (adjoint = 1): 0 none yet (or no nodes), 1 groups of nodes
- * per warp (FP32-mixed B), 2 one warp per node over a tile, 3 lines of tiles
- * (B^T), 4 one thread per node.  Set when the launch is issued. */
+ * per warp (FP32-mixed B), 2 one warp per node over a tile, 3 lines of tiles,
+ * 4 one thread per node.  Set when the launch is issued. */
 int pnfft_gb300_get_conv_kernel(const pnfft_plan ths, int adjoint);
 
 /* Zero-copy mode.  When device arrays are attached, pnfft_trafo/pnfft_adj read

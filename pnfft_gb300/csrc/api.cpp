@@ -891,8 +891,9 @@ extern "C" int pnfft_gb300_set_precision(pnfft_plan ths, int precision) {
 extern "C" int pnfft_gb300_get_precision(const pnfft_plan ths) { return ths ? ths->precision : -1; }
 extern "C" int pnfft_gb300_set_conv_method(pnfft_plan ths, int method) {
   if (!ths) return -1;
-  if (method < 0 || method > 2) {
-    set_error("pnfft_gb300_set_conv_method: unknown method %d (0: tiled, 1: per node, 2: tiled, ungrouped)",
+  if (method < 0 || method > 3) {
+    set_error("pnfft_gb300_set_conv_method: unknown method %d (0: lines / tiles, 1: per node, 2: one warp per "
+              "node, 3: grouped)",
               method);
     return -1;
   }

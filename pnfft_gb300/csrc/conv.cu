@@ -1,6 +1,8 @@
 // conv.cu -- the convolution with the window: the binning of nodes onto
 // grid tiles, and the dispatch of interpolation B (grid -> nodes,
 // pnfft_trafo) and spreading B^T (nodes -> grid, pnfft_adj) to the kernels:
+//   * interp_line.cu: FP32-mixed B (f only) over lines of tiles with
+//     register-resident grid columns (the transpose of the spreading);
 //   * interp_group.cu: FP32-mixed B (f only), groups of nodes per warp;
 //   * interp_tile.cuh (interp_tile_f32.cu, interp_tile_f64.cu): B, one warp
 //     per node over a shared-memory copy of the tile's region;
@@ -290,22 +292,26 @@ void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 // dispatch
 // ---------------------------------------------------------------------------
-void choose_tiles(int cut, bool fp32, bool spread, const int *n, int64_t M, int *T, int *line_mode) {
-  // interpolation: 8x8x8 cells per tile, the CTA stages the (8+2m)^3 region
-  // in shared memory (FP64, m=7: 170 KB).  Spreading: lines of 4x4x4-cell
-  // tiles along axis 2 (k_spread_line); the record packs u2 in 15 bits.
+void choose_tiles(int cut, bool fp32, bool spread, bool f_only, int method, const int *n, int64_t M, int *T,
+                  int *line_mode) {
+  // Spreading, and the FP32-mixed interpolation of f alone (method 0): lines
+  // of 4x4x4-cell tiles along axis 2 (k_spread_line, k_interp_line; the
+  // record packs u2 in 15 bits).  Other interpolations: 8x8x8 cells per
+  // tile, the CTA stages the (8+2m)^3 region in shared memory (FP64, m=7:
+  // 170 KB).
   *line_mode = BIN_TILE;
-  if (spread && cut <= 15 && n[0] >= 4 && n[1] >= 4 && n[2] >= 4 && n[2] < 32768) {
+  const bool lines_fit = n[0] >= 4 && n[1] >= 4 && n[2] >= 4 && n[2] < 32768;
+  if (lines_fit && ((spread && cut <= 15) || (!spread && fp32 && f_only && method == 0 && cut <= 13))) {
     T[0] = T[1] = T[2] = 4;
     *line_mode = BIN_LINE;
     return;
   }
   for (int d = 0; d < 3; d++) T[d] = n[d] >= 8 ? 8 : n[d];
-  // FP32-mixed interpolation groups the nodes of 2x2x4 corner blocks when
-  // there are enough of them (on average half a node per block or more);
-  // a group's z extent, cut + 3, must fit the 16 lanes of a half-warp
+  // method 3: the FP32-mixed interpolation groups the nodes of 2x2x4 corner
+  // blocks when there are enough of them (on average half a node per block
+  // or more); a group's z extent, cut + 3, must fit the 16 lanes of a half-warp
   const int64_t ntiles = (int64_t)((n[0] + 7) / 8) * ((n[1] + 7) / 8) * ((n[2] + 7) / 8);
-  if (!spread && fp32 && cut <= 13 && T[0] == 8 && T[1] == 8 && T[2] == 8 &&
+  if (!spread && fp32 && method == 3 && cut <= 13 && T[0] == 8 && T[1] == 8 && T[2] == 8 &&
       ntiles * kBlocksPerTile < (1 << 30) && 2 * M >= ntiles * kBlocksPerTile)
     *line_mode = BIN_GROUP;
 }
@@ -318,7 +324,9 @@ static bool tiles_usable(const ConvArgs &a) {
 
 int launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s) {
   if (a.M == 0) return CONV_NONE;
-  if (fp32 && mode == 1 && !a.generic && !a.no_group && a.bin.line_mode == BIN_GROUP && tiles_usable(a) &&
+  if (fp32 && mode == 1 && !a.generic && a.bin.line_mode == BIN_LINE && tiles_usable(a) && launch_interp_line(a, s))
+    return CONV_LINE;
+  if (fp32 && mode == 1 && !a.generic && a.bin.line_mode == BIN_GROUP && tiles_usable(a) &&
       a.bin.sub_max <= kGroupSubMax && launch_interp_group(a, s))
     return CONV_GROUP;
   if (!a.generic && a.bin.line_mode != BIN_LINE && tiles_usable(a) &&

@@ -313,12 +313,12 @@ static void free_binning(Binning &b) {
   b.bsum = nullptr;
 }
 
-static int ensure_binning(pnfft_plan p, int64_t M, int spread, int il) {
+static int ensure_binning(pnfft_plan p, int64_t M, int spread, int il, bool f_only) {
   DevState *d = p->dev;
   DevState::BinSlot &sl = d->bins[spread][il];
   int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
   int T[3], line_mode = 0;
-  choose_tiles(p->cutoff, fp32(p), spread != 0, n, M, T, &line_mode);
+  choose_tiles(p->cutoff, fp32(p), spread != 0, f_only, p->conv_method, n, M, T, &line_mode);
   bool same = T[0] == sl.T[0] && T[1] == sl.T[1] && T[2] == sl.T[2] && line_mode == sl.line_mode;
   if (same && sl.cap >= M && sl.b.key && sl.prec == p->precision) return 0;
   int64_t cap = std::max<int64_t>(M, std::max<int64_t>(sl.cap, 1));
@@ -495,10 +495,10 @@ static int fft_exec(pnfft_plan p, int direction) {
 }
 
 // bins the nodes for pass `il` unless a valid binning of the same fixed nodes exists
-static int do_binning(pnfft_plan p, pnfft_nodes nd, ConvArgs &a, int il, int adj, cudaStream_t s = nullptr) {
+static int do_binning(pnfft_plan p, pnfft_nodes nd, ConvArgs &a, int il, int adj, cudaStream_t s, bool f_only) {
   DevState *d = p->dev;
   if (!s) s = d->stream;
-  if (ensure_binning(p, nd->local_M, adj, il)) return -1;
+  if (ensure_binning(p, nd->local_M, adj, il, f_only)) return -1;
   DevState::BinSlot &sl = d->bins[adj][il];
   a.bin = sl.b;
   bool reuse = nd->fixed && sl.valid && sl.uid == nd->uid && sl.ver == nd->version;
@@ -713,11 +713,12 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       const bool il_plan = (p->pnfft_flags & PNFFT_INTERLACED) != 0;
       const bool ik = (p->pnfft_flags & PNFFT_DIFF_IK) != 0;
       const bool f32 = fp32(p);
+      // every interpolation of this call computes f alone (ik: one pass per component)
+      const bool f_only = ik || !(cflags & (C_GRAD | C_HESS));
       ConvArgs ca;
       memset(&ca, 0, sizeof(ca));
       ca.w = window_args(p);
       ca.generic = p->conv_method == 1;
-      ca.no_group = p->conv_method == 2;
       ca.real_only = p->c2r || (p->pnfft_flags & PNFFT_PRE_QUAD_PSI) ? 1 : 0;
       ca.real_io = p->c2r;
       ca.M = M;
@@ -729,7 +730,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       if (fork) {
         for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
           ca.il = il_plan ? pass : 0;
-          if (do_binning(p, nd, ca, ca.il, 0, d->aux)) return -1;
+          if (do_binning(p, nd, ca, ca.il, 0, d->aux, f_only)) return -1;
           pass_bin[pass] = ca.bin;
         }
       }
@@ -875,7 +876,6 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       memset(&ca, 0, sizeof(ca));
       ca.w = window_args(p);
       ca.generic = p->conv_method == 1;
-      ca.no_group = p->conv_method == 2;
       ca.real_only = 0;
       ca.real_io = p->c2r;
       ca.M = M;
@@ -887,7 +887,7 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       if (fork) {
         for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
           ca.il = il_plan ? pass : 0;
-          if (do_binning(p, nd, ca, ca.il, 1, d->aux)) return -1;
+          if (do_binning(p, nd, ca, ca.il, 1, d->aux, true)) return -1;
           pass_bin[pass] = ca.bin;
         }
       }

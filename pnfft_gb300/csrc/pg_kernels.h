@@ -34,7 +34,7 @@ constexpr int kPolyCoef = 16;
 // of the nodes of one line of tiles along axis 2 (the tiles with the same
 // t0, t1, which the sort keeps consecutive and in slab order), and the
 // records carry the full lowest z index u2 instead of the in-tile offset.
-// In group mode (FP32-mixed interpolation) the sort key is finer: the tile
+// In group mode (FP32-mixed interpolation, conv method 3) the sort key is finer: the tile
 // and the 2x2x4 block of stencil corners within it (32 keys per tile), and
 // the record of every kGroupMax-th node of a block (by rank) carries a
 // group-start bit, so that the nodes of one block are consecutive and cut
@@ -76,7 +76,6 @@ struct ConvArgs {
   int real_io;      // node arrays are real (c2r) instead of complex
   int accum;        // add into the node outputs (else store): ACCUMULATED, 2nd interlaced pass
   int generic;      // use the one-thread-per-node kernels (set per plan, e.g. by an autotuner)
-  int no_group;     // FP32-mixed interpolation: one warp per node also on a group-mode binning
   int64_t M;
   const double *x;  // [M][3]
   void *grid;       // n0*n1*n2 complex in compute precision, natural order
@@ -96,6 +95,8 @@ int launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
 int launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
 // Kernel families behind launch_interp / launch_spread; each returns false
 // when it has no instance for the cutoff or mode.
+// FP32-mixed f-only interpolation on a BIN_LINE binning (interp_line.cu)
+bool launch_interp_line(const ConvArgs &a, cudaStream_t s);
 // FP32-mixed f-only interpolation on a BIN_GROUP binning (interp_group.cu)
 bool launch_interp_group(const ConvArgs &a, cudaStream_t s);
 // one warp per node on tile binnings (interp_tile_f32.cu, interp_tile_f64.cu)
@@ -108,8 +109,10 @@ bool launch_spread_line_f64(const ConvArgs &a, int mode, cudaStream_t s);
 void launch_interp_generic(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
 void launch_spread_generic(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
 // Tile shape and BinMode of the binning for interpolation (spread = false)
-// or spreading (spread = true).
-void choose_tiles(int cut, bool fp32, bool spread, const int *n, int64_t M, int *T, int *line_mode);
+// or spreading (spread = true); f_only: the interpolation computes f alone
+// (no gradient or Hessian in the same pass); method: the plan's conv method.
+void choose_tiles(int cut, bool fp32, bool spread, bool f_only, int method, const int *n, int64_t M, int *T,
+                  int *line_mode);
 
 // Deconvolution (deconv.cu).
 struct DeconvArgs {

@@ -25,11 +25,11 @@ def declared_functions():
 
 
 def test_conv_kernel_query_before_any_transform(lib):
-    # no B / B^T launched yet; conv methods outside 0..2 are refused
+    # no B / B^T launched yet; conv methods outside 0..3 are refused
     p = lib.Plan((8, 8, 8), m=3)
     assert p.conv_kernel() == "none" and p.conv_kernel(adjoint=True) == "none"
     with pytest.raises(lib.PnfftError):
-        p.set_conv_method(3)
+        p.set_conv_method(4)
     p.set_conv_method(2)
     assert lib.load().pnfft_gb300_get_conv_method(p._p) == 2
     p.close()
