@@ -58,7 +58,8 @@ int pnfft_gb300_set_stream(pnfft_plan ths, void *cuda_stream);
  *      the same lines, other B one warp per node over a tile (cutoff and
  *      grid permitting);
  *  1 = one thread per node (small node counts on large grids);
- *  2 = B one warp per node over a tile also for the FP32-mixed f;
+ *  2 = B one warp per node over a tile also for the FP32-mixed f, and the
+ *      FP32-mixed B^T of f with the register window that moves by copies;
  *  3 = the FP32-mixed B of f in groups of nodes with overlapping stencils
  *      per warp (the same bits as 2). */
 int pnfft_gb300_set_conv_method(pnfft_plan ths, int method);

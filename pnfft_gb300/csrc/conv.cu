@@ -6,8 +6,10 @@
 //   * interp_group.cu: FP32-mixed B (f only), groups of nodes per warp;
 //   * interp_tile.cuh (interp_tile_f32.cu, interp_tile_f64.cu): B, one warp
 //     per node over a shared-memory copy of the tile's region;
+//   * spread_line_f.cu: FP32-mixed B^T of f alone over lines of tiles with a
+//     rotating register window of grid columns;
 //   * spread_line.cuh (spread_line_f32.cu, spread_line_f64.cu): B^T over
-//     lines of tiles with register-resident grid columns;
+//     lines of tiles with register-resident grid columns (FP64, gradients);
 //   * generic.cu: one thread per node, any cutoff and grid.
 //
 // Reference: loop_over_particles_trafo / _adj (kernel/ndft-parallel.c:2703-3009)
@@ -338,6 +340,9 @@ int launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s) {
 
 int launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s) {
   if (a.M == 0) return CONV_NONE;
+  if (fp32 && mode == 1 && a.method == 0 && a.bin.line_mode == BIN_LINE && tiles_usable(a) &&
+      launch_spread_line_f(a, s))
+    return CONV_LINE;
   if (!a.generic && a.bin.line_mode == BIN_LINE && tiles_usable(a) &&
       (fp32 ? launch_spread_line_f32(a, mode, s) : launch_spread_line_f64(a, mode, s)))
     return CONV_LINE;

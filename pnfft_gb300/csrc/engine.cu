@@ -719,6 +719,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       memset(&ca, 0, sizeof(ca));
       ca.w = window_args(p);
       ca.generic = p->conv_method == 1;
+      ca.method = p->conv_method;
       ca.real_only = p->c2r || (p->pnfft_flags & PNFFT_PRE_QUAD_PSI) ? 1 : 0;
       ca.real_io = p->c2r;
       ca.M = M;
@@ -876,6 +877,7 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       memset(&ca, 0, sizeof(ca));
       ca.w = window_args(p);
       ca.generic = p->conv_method == 1;
+      ca.method = p->conv_method;
       ca.real_only = 0;
       ca.real_io = p->c2r;
       ca.M = M;

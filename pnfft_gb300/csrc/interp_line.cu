@@ -6,9 +6,7 @@
 // with the interpolation loops of kernel/assign.c:667-691.
 #include <cuda_runtime.h>
 
-#include "pg_conv.cuh"
-#include "pg_kernels.h"
-#include "pg_math.cuh"
+#include "line_f32.cuh"
 
 namespace pg {
 
@@ -27,65 +25,87 @@ namespace pg {
 // psi_y[b + R/2] s_1); the shares of all threads are added in a fixed order
 // in shared memory (four threads per node, then two shuffles), so a node's
 // result depends only on the node.
-// Window values are evaluated stencil-point-major (a warp takes one stencil
-// point of one axis for 32 nodes, so the fitted polynomial's coefficients
-// are broadcast reads) into zeroed rows: the node's z row in slot rotation,
-// its x row over the region's rows and its y row over the region's column
-// pairs.
+// Window values: one thread per (axis, node) evaluates the node's CUT values
+// on that axis (a warp shares the axis, so the fitted polynomials'
+// coefficients are broadcast reads) into its row: the z row in slot rotation
+// (zero outside the stencil), the x row over the region's rows and the y row
+// over the region's column pairs.  Nodes of one slab go through the z sums
+// in pairs (8 independent FMA chains), and the group of z values that the
+// next slab brings in is prefetched with cp.async.
 // ---------------------------------------------------------------------------
-template <int CUT>
-struct ILGeom {
-  static constexpr int TL = 4;                   // tile edge in every axis
-  static constexpr int R = TL + CUT - 1;         // region edge in axes 0, 1
-  static constexpr int HR = R / 2;               // column pairs per region row
-  static constexpr int W = (CUT + TL - 1 <= 8) ? 8 : 16;  // z slots (power of two)
-  static constexpr int NG = W / 4;               // groups of 4 slots
-  static constexpr int THREADS = (R * HR + 31) / 32 * 32;
-  static constexpr int NB = THREADS / 4;         // nodes per batch: 4 threads reduce each
-  static constexpr int WS = W + 32 + 4;          // floats per node row (z slots, x rows, y pairs, pad)
-  static constexpr int PS = 20;                  // shared-memory stride of a polynomial row (16 used)
-  static constexpr int PR = THREADS + 4;         // float2 per node row of the shares
-  static_assert(R % 2 == 0 && R <= 16, "region rows and column pairs fit the staged rows");
-  static_assert(CUT + TL - 1 <= W, "a slab's stencils fit the z window");
-  static_assert(WS % 4 == 0, "16-byte aligned node rows");
-};
-
-__device__ __forceinline__ int wrap_n(int z, int n) {
-  if (z >= n) z -= n;
-  if (z >= n) z %= n;
-  return z;
+// z sums of the two columns for one node: 4 independent FFMA2 chains
+template <int NG>
+__device__ __forceinline__ void zsum(const float2 *g0, const float2 *g1, const float4 *pz4, float2 &s0, float2 &s1) {
+  float2 s0a = make_float2(0.f, 0.f), s0b = s0a, s1a = s0a, s1b = s0a;
+#pragma unroll
+  for (int q = 0; q < NG; q++) {
+    const float4 z = pz4[q];
+    s0a = __ffma2_rn(g0[4 * q], make_float2(z.x, z.x), s0a);
+    s1a = __ffma2_rn(g1[4 * q], make_float2(z.x, z.x), s1a);
+    s0b = __ffma2_rn(g0[4 * q + 1], make_float2(z.y, z.y), s0b);
+    s1b = __ffma2_rn(g1[4 * q + 1], make_float2(z.y, z.y), s1b);
+    s0a = __ffma2_rn(g0[4 * q + 2], make_float2(z.z, z.z), s0a);
+    s1a = __ffma2_rn(g1[4 * q + 2], make_float2(z.z, z.z), s1a);
+    s0b = __ffma2_rn(g0[4 * q + 3], make_float2(z.w, z.w), s0b);
+    s1b = __ffma2_rn(g1[4 * q + 3], make_float2(z.w, z.w), s1b);
+  }
+  s0 = __fadd2_rn(s0a, s0b);
+  s1 = __fadd2_rn(s1a, s1b);
 }
 
-// loads the 4 z values z0 .. z0+3 (wrapped) of a grid column into v[0..3]
-__device__ __forceinline__ void load_z4(const float2 *__restrict__ col, int z0, int n2, bool vec, int real_only,
-                                        float2 *v) {
-  if (vec) {  // n2 % 4 == 0: z0 wraps to a multiple of 4, the 4 values are contiguous and 32-byte aligned
-    const float4 *p = (const float4 *)(col + wrap_n(z0, n2));
-    const float4 a = __ldg(p), b = __ldg(p + 1);
-    v[0] = make_float2(a.x, a.y);
-    v[1] = make_float2(a.z, a.w);
-    v[2] = make_float2(b.x, b.y);
-    v[3] = make_float2(b.z, b.w);
-  } else {
+// the same for two nodes of one slab: 8 independent chains
+template <int NG>
+__device__ __forceinline__ void zsum2(const float2 *g0, const float2 *g1, const float4 *pa, const float4 *pb,
+                                      float2 &a0, float2 &a1, float2 &b0, float2 &b1) {
+  float2 a0a = make_float2(0.f, 0.f), a0b = a0a, a1a = a0a, a1b = a0a, b0a = a0a, b0b = a0a, b1a = a0a, b1b = a0a;
 #pragma unroll
-    for (int k = 0; k < 4; k++) v[k] = __ldg(col + wrap_n(z0 + k, n2));
+  for (int q = 0; q < NG; q++) {
+    const float4 y = pa[q], z = pb[q];
+    a0a = __ffma2_rn(g0[4 * q], make_float2(y.x, y.x), a0a);
+    a1a = __ffma2_rn(g1[4 * q], make_float2(y.x, y.x), a1a);
+    b0a = __ffma2_rn(g0[4 * q], make_float2(z.x, z.x), b0a);
+    b1a = __ffma2_rn(g1[4 * q], make_float2(z.x, z.x), b1a);
+    a0b = __ffma2_rn(g0[4 * q + 1], make_float2(y.y, y.y), a0b);
+    a1b = __ffma2_rn(g1[4 * q + 1], make_float2(y.y, y.y), a1b);
+    b0b = __ffma2_rn(g0[4 * q + 1], make_float2(z.y, z.y), b0b);
+    b1b = __ffma2_rn(g1[4 * q + 1], make_float2(z.y, z.y), b1b);
+    a0a = __ffma2_rn(g0[4 * q + 2], make_float2(y.z, y.z), a0a);
+    a1a = __ffma2_rn(g1[4 * q + 2], make_float2(y.z, y.z), a1a);
+    b0a = __ffma2_rn(g0[4 * q + 2], make_float2(z.z, z.z), b0a);
+    b1a = __ffma2_rn(g1[4 * q + 2], make_float2(z.z, z.z), b1a);
+    a0b = __ffma2_rn(g0[4 * q + 3], make_float2(y.w, y.w), a0b);
+    a1b = __ffma2_rn(g1[4 * q + 3], make_float2(y.w, y.w), a1b);
+    b0b = __ffma2_rn(g0[4 * q + 3], make_float2(z.w, z.w), b0b);
+    b1b = __ffma2_rn(g1[4 * q + 3], make_float2(z.w, z.w), b1b);
   }
-  if (real_only) {
-#pragma unroll
-    for (int k = 0; k < 4; k++) v[k].y = 0.f;
-  }
+  a0 = __fadd2_rn(a0a, a0b);
+  a1 = __fadd2_rn(a1a, a1b);
+  b0 = __fadd2_rn(b0a, b0b);
+  b1 = __fadd2_rn(b1a, b1b);
+}
+
+// the thread's share of a node: psi_x[a] (psi_y[b] s0 + psi_y[b + R/2] s1)
+template <int W>
+__device__ __forceinline__ float2 share(const float *row, int ca, int cb, float2 s0, float2 s1) {
+  const float px = row[W + ca];
+  const float2 py = ((const float2 *)(row + W + 16))[cb];
+  float2 t = __fmul2_rn(s0, make_float2(py.x, py.x));
+  t = __ffma2_rn(s1, make_float2(py.y, py.y), t);
+  return __fmul2_rn(t, make_float2(px, px));
 }
 
 template <int CUT>
-__global__ void __launch_bounds__(ILGeom<CUT>::THREADS, 4) k_interp_line(ConvArgs a) {
-  typedef ILGeom<CUT> G;
+__global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 4) k_interp_line(ConvArgs a) {
+  typedef LineGeom32<CUT> G;
   constexpr int TL = G::TL, R = G::R, HR = G::HR, W = G::W, NG = G::NG, NB = G::NB, WS = G::WS, PS = G::PS,
                 PR = G::PR, NTH = G::THREADS;
+  constexpr bool ALL_ACTIVE = R * HR == NTH;
   __shared__ __align__(16) float s_w[NB][WS];
   __shared__ __align__(16) float2 s_part[NB][PR];
   __shared__ __align__(16) float s_poly[3 * CUT * PS];
+  __shared__ __align__(16) float2 s_pre[NTH][8];  // prefetched next group of z values, per thread
   __shared__ float s_d[NB][3];
-  __shared__ int s_o[NB], s_j[NB];
+  __shared__ int s_o[NB], s_j[NB], s_slab[NB];
   const Binning &b = a.bin;
   const int sub = blockIdx.x;
   if (sub >= *b.nsub) return;
@@ -93,13 +113,15 @@ __global__ void __launch_bounds__(ILGeom<CUT>::THREADS, 4) k_interp_line(ConvArg
   if (cnt <= 0) return;  // a line without nodes
   const int t1 = line % b.ntile[1], t0 = line / b.ntile[1];
   const int tid = threadIdx.x;
-  const bool active = tid < R * HR;
+  const bool active = ALL_ACTIVE || tid < R * HR;
   const int ca = active ? tid / HR : 0, cb = active ? tid % HR : 0;
   const int n0 = a.w.n[0], n1 = a.w.n[1], n2 = a.w.n[2];
   const size_t gx = (size_t)((t0 * TL + ca) % n0) * n1;
   const float2 *grid = (const float2 *)a.grid;
   const float2 *col0 = grid + (gx + (t1 * TL + cb) % n1) * n2;
   const float2 *col1 = grid + (gx + (t1 * TL + cb + HR) % n1) * n2;
+  // n2 % 4 == 0: a group of 4 z values is contiguous and 32-byte aligned, and
+  // the next slab's group is prefetched with cp.async
   const bool vec = (n2 & 3) == 0;
   const WindowArgs &w = a.w;
   const bool poly = w.poly && w.intpol_order < 0;
@@ -107,94 +129,120 @@ __global__ void __launch_bounds__(ILGeom<CUT>::THREADS, 4) k_interp_line(ConvArg
     for (int i = tid; i < 3 * CUT * 4; i += NTH)
       ((float4 *)(s_poly + (i >> 2) * PS))[i & 3] = __ldg((const float4 *)(w.poly + (i >> 2) * kPolyCoef) + (i & 3));
   const float scale = a.use_il ? 0.5f : 1.f;
+  float2 *pre = s_pre[tid];
 
   float2 g0[W], g1[W];  // the two columns' z windows, slot p holds z = p (mod W)
 #pragma unroll
   for (int p = 0; p < W; p++) g0[p] = g1[p] = make_float2(0.f, 0.f);
-  int zs = -1;  // slab of the window (-1: none loaded)
+  int zs = -1;          // slab of the window (-1: none loaded)
+  bool pending = false;  // a prefetch of the group for slab zs + 1 is in flight
 
   for (int b0 = 0; b0 < cnt; b0 += NB) {
     const int nb = min(NB, cnt - b0);
     __syncthreads();  // the previous batch's rows and shares are consumed
-    // --- stage the node records and clear the window rows ---------------------
+    // --- stage the node records ------------------------------------------------
     if (tid < nb) {
       const float4 r = ((const float4 *)b.rec)[first + b0 + tid];
       s_d[tid][0] = r.x;
       s_d[tid][1] = r.y;
       s_d[tid][2] = r.z;
-      s_o[tid] = __float_as_int(r.w);
+      const int pk = __float_as_int(r.w);
+      s_o[tid] = pk;
+      s_slab[tid] = ((pk >> 16) & 0x7fff) >> 2;
       s_j[tid] = b.perm[first + b0 + tid];
     }
-    for (int v = tid; v < nb * (WS / 4); v += NTH) ((float4 *)&s_w[0][0])[v] = make_float4(0.f, 0.f, 0.f, 0.f);
     __syncthreads();
-    // --- window values, stencil-point-major -------------------------------------
-    for (int v = tid; v < 3 * CUT * NB; v += NTH) {
-      const int e = v / NB, i = v - e * NB;
-      if (i >= nb) continue;
-      const int t = e / CUT, c = e - t * CUT;
-      const float dist = s_d[i][t];
-      float val;
-      if (poly && !(w.kind == WIN_BESSEL_I0 && c == 0 && dist == 0.f)) {
-        const float4 *rw = (const float4 *)(s_poly + e * PS);
-        val = w.poly_ncoef <= 12 ? poly_horner12(rw[0], rw[1], rw[2], dist - 0.5f)
-                                 : poly_horner(rw[0], rw[1], rw[2], rw[3], dist - 0.5f);
-      } else {
-        float out[3];
-        window_point<float>(w, t, c, dist, 0, out);
-        val = out[0];
+    // --- window rows: one thread per (axis, node) ----------------------------------
+    if (tid < 3 * NB) {
+      const int t = tid / NB, i = tid - t * NB;  // a warp shares the axis: broadcast polynomial rows
+      if (i < nb) {
+        float v[CUT];
+        window_row<CUT>(w, poly, s_poly, t, s_d[i][t], v);
+        const int pk = s_o[i];
+        float *row = s_w[i];
+        if (t == 2) {  // z slots in the window's rotation; the W - CUT others are zero
+          const int u2 = (pk >> 16) & 0x7fff;
+#pragma unroll
+          for (int c = 0; c < W; c++) row[(u2 + c) & (W - 1)] = c < CUT ? v[c] : 0.f;
+        } else if (t == 0) {  // region rows
+          const int o0 = pk & 0xff;
+#pragma unroll
+          for (int q = 0; q < 4; q++) ((float4 *)(row + W))[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int c = 0; c < CUT; c++) row[W + o0 + c] = v[c];
+        } else {  // region columns as (b, b + R/2) pairs
+          const int o1 = (pk >> 8) & 0xff;
+#pragma unroll
+          for (int q = 0; q < 4; q++) ((float4 *)(row + W + 16))[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+          for (int c = 0; c < CUT; c++) {
+            const int bc = o1 + c;
+            row[W + 16 + 2 * (bc < HR ? bc : bc - HR) + (bc < HR ? 0 : 1)] = v[c];
+          }
+        }
       }
-      const int pk = s_o[i];
-      int pos;
-      if (t == 2) {
-        pos = (((pk >> 16) & 0x7fff) + c) & (W - 1);  // z slot
-      } else if (t == 0) {
-        pos = W + (pk & 0xff) + c;  // region row
-      } else {
-        const int bc = ((pk >> 8) & 0xff) + c;  // region column -> (pair, element)
-        pos = W + 16 + 2 * (bc % HR) + bc / HR;
-      }
-      s_w[i][pos] = val;
     }
     __syncthreads();
-    // --- the z sums of the thread's two columns, node by node --------------------
-    for (int i = 0; i < nb; i++) {
-      const int slab = ((s_o[i] >> 16) & 0x7fff) >> 2;
+    // --- the z sums of the thread's two columns, nodes of one slab in pairs -------
+    for (int i = 0; i < nb;) {
+      const int slab = s_slab[i];
       if (slab != zs) {
-        // group q of the new window holds z = 4 (slab + ((q - slab) mod NG)); it
-        // is loaded unless the old window already holds it
+        if (active) {
+          // group q of the new window holds z = 4 (slab + ((q - slab) mod NG))
+          const bool next = pending && slab == zs + 1;
+          if (pending) cp_async_wait_all();  // also before the slot is refilled after a jump
 #pragma unroll
-        for (int q = 0; q < NG; q++) {
-          const int zq = 4 * (slab + ((q - slab) & (NG - 1)));
-          if (zs < 0 || zq >= 4 * zs + W) {
-            if (active) {
-              load_z4(col0, zq, n2, vec, a.real_only, &g0[4 * q]);
-              load_z4(col1, zq, n2, vec, a.real_only, &g1[4 * q]);
+          for (int q = 0; q < NG; q++) {
+            const int zq = 4 * (slab + ((q - slab) & (NG - 1)));
+            if (zs < 0 || zq >= 4 * zs + W) {
+              if (next) {  // the only new group, prefetched
+                const float4 *pp = (const float4 *)pre;
+                const float4 u0 = pp[0], u1 = pp[1], u2 = pp[2], u3 = pp[3];
+                g0[4 * q] = make_float2(u0.x, u0.y);
+                g0[4 * q + 1] = make_float2(u0.z, u0.w);
+                g0[4 * q + 2] = make_float2(u1.x, u1.y);
+                g0[4 * q + 3] = make_float2(u1.z, u1.w);
+                g1[4 * q] = make_float2(u2.x, u2.y);
+                g1[4 * q + 1] = make_float2(u2.z, u2.w);
+                g1[4 * q + 2] = make_float2(u3.x, u3.y);
+                g1[4 * q + 3] = make_float2(u3.z, u3.w);
+                if (a.real_only) {
+#pragma unroll
+                  for (int k = 0; k < 4; k++) g0[4 * q + k].y = g1[4 * q + k].y = 0.f;
+                }
+              } else {
+                load_z4(col0, zq, n2, vec, a.real_only, &g0[4 * q]);
+                load_z4(col1, zq, n2, vec, a.real_only, &g1[4 * q]);
+              }
             }
+          }
+          pending = false;
+          if (vec) {  // the group that the next slab brings in
+            const int zn = wrap_n(4 * slab + W, n2);
+            cp_async16(pre, col0 + zn);
+            cp_async16(pre + 2, col0 + zn + 2);
+            cp_async16(pre + 4, col1 + zn);
+            cp_async16(pre + 6, col1 + zn + 2);
+            cp_async_commit();
+            pending = true;
           }
         }
         zs = slab;
       }
-      const float4 *pz4 = (const float4 *)s_w[i];
-      float2 s0a = make_float2(0.f, 0.f), s0b = s0a, s1a = s0a, s1b = s0a;
-#pragma unroll
-      for (int q = 0; q < NG; q++) {
-        const float4 z = pz4[q];
-        s0a = __ffma2_rn(g0[4 * q], make_float2(z.x, z.x), s0a);
-        s1a = __ffma2_rn(g1[4 * q], make_float2(z.x, z.x), s1a);
-        s0b = __ffma2_rn(g0[4 * q + 1], make_float2(z.y, z.y), s0b);
-        s1b = __ffma2_rn(g1[4 * q + 1], make_float2(z.y, z.y), s1b);
-        s0a = __ffma2_rn(g0[4 * q + 2], make_float2(z.z, z.z), s0a);
-        s1a = __ffma2_rn(g1[4 * q + 2], make_float2(z.z, z.z), s1a);
-        s0b = __ffma2_rn(g0[4 * q + 3], make_float2(z.w, z.w), s0b);
-        s1b = __ffma2_rn(g1[4 * q + 3], make_float2(z.w, z.w), s1b);
+      if (i + 1 < nb && s_slab[i + 1] == slab) {
+        float2 a0, a1, c0, c1;
+        zsum2<NG>(g0, g1, (const float4 *)s_w[i], (const float4 *)s_w[i + 1], a0, a1, c0, c1);
+        const float2 ta = share<W>(s_w[i], ca, cb, a0, a1), tb = share<W>(s_w[i + 1], ca, cb, c0, c1);
+        s_part[i][tid] = active ? ta : make_float2(0.f, 0.f);
+        s_part[i + 1][tid] = active ? tb : make_float2(0.f, 0.f);
+        i += 2;
+      } else {
+        float2 s0, s1;
+        zsum<NG>(g0, g1, (const float4 *)s_w[i], s0, s1);
+        const float2 t = share<W>(s_w[i], ca, cb, s0, s1);
+        s_part[i][tid] = active ? t : make_float2(0.f, 0.f);
+        i += 1;
       }
-      const float px = s_w[i][W + ca];
-      const float2 py = ((const float2 *)(s_w[i] + W + 16))[cb];
-      const float2 s0 = __fadd2_rn(s0a, s0b), s1 = __fadd2_rn(s1a, s1b);
-      float2 t = __fmul2_rn(s0, make_float2(py.x, py.x));
-      t = __ffma2_rn(s1, make_float2(py.y, py.y), t);
-      t = __fmul2_rn(t, make_float2(px, px));
-      s_part[i][tid] = active ? t : make_float2(0.f, 0.f);
     }
     __syncthreads();
     // --- the node sums: four threads per node, a fixed order -----------------------
@@ -229,11 +277,12 @@ __global__ void __launch_bounds__(ILGeom<CUT>::THREADS, 4) k_interp_line(ConvArg
       }
     }
   }
+  if (pending) cp_async_wait_all();  // no copy outlives the CTA
 }
 
 template <int CUT>
 static void run_interp_line(const ConvArgs &a, cudaStream_t s) {
-  k_interp_line<CUT><<<a.bin.max_subs, ILGeom<CUT>::THREADS, 0, s>>>(a);
+  k_interp_line<CUT><<<a.bin.max_subs, LineGeom32<CUT>::THREADS, 0, s>>>(a);
 }
 
 bool launch_interp_line(const ConvArgs &a, cudaStream_t s) {

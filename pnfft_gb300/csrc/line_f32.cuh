@@ -1,0 +1,91 @@
+// line_f32.cuh -- shared pieces of the FP32-mixed line kernels of f alone:
+// the interpolation B (interp_line.cu) and the spreading B^T
+// (spread_line_f.cu).  One CTA takes the nodes of one line of 4x4x4-cell
+// tiles along axis 2 (sorted by slab = u2 / 4); thread (a, b) owns the grid
+// columns (a, b) and (a, b + R/2) of the line's (3+CUT)^2 region and keeps W
+// consecutive z values of each in registers, in rotation: slot p holds the
+// z of the window with z = p (mod W), and the window of slab s covers z in
+// [4s, 4s + W).  A node's z row is staged in the same rotation, so every
+// column update or z sum is one branch-free run over the W slots.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "pg_conv.cuh"
+#include "pg_kernels.h"
+#include "pg_math.cuh"
+
+namespace pg {
+
+template <int CUT>
+struct LineGeom32 {
+  static constexpr int TL = 4;                   // tile edge in every axis
+  static constexpr int R = TL + CUT - 1;         // region edge in axes 0, 1
+  static constexpr int HR = R / 2;               // column pairs per region row
+  static constexpr int W = (CUT + TL - 1 <= 8) ? 8 : 16;  // z slots (power of two)
+  static constexpr int NG = W / 4;               // groups of 4 slots
+  static constexpr int THREADS = (R * HR + 31) / 32 * 32;
+  static constexpr int NB = THREADS / 4;         // nodes per batch: 4 threads reduce each
+  static constexpr int WS = W + 32 + 4;          // floats per node row (z slots, x rows, y pairs, pad)
+  static constexpr int PS = 20;                  // shared-memory stride of a polynomial row (16 used)
+  static constexpr int PR = THREADS + 4;         // float2 per node row of the shares
+  static_assert(R % 2 == 0 && R <= 16, "region rows and column pairs fit the staged rows");
+  static_assert(CUT + TL - 1 <= W, "a slab's stencils fit the z window");
+  static_assert(WS % 4 == 0, "16-byte aligned node rows");
+};
+
+__device__ __forceinline__ int wrap_n(int z, int n) {
+  if (z >= n) z -= n;
+  if (z >= n) z %= n;
+  return z;
+}
+
+// loads the 4 z values z0 .. z0+3 (wrapped) of a grid column into v[0..3]
+__device__ __forceinline__ void load_z4(const float2 *__restrict__ col, int z0, int n2, bool vec, int real_only,
+                                        float2 *v) {
+  if (vec) {  // n2 % 4 == 0: z0 wraps to a multiple of 4, the 4 values are contiguous and 32-byte aligned
+    const float4 *p = (const float4 *)(col + wrap_n(z0, n2));
+    const float4 a = __ldg(p), b = __ldg(p + 1);
+    v[0] = make_float2(a.x, a.y);
+    v[1] = make_float2(a.z, a.w);
+    v[2] = make_float2(b.x, b.y);
+    v[3] = make_float2(b.z, b.w);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = __ldg(col + wrap_n(z0 + k, n2));
+  }
+  if (real_only) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k].y = 0.f;
+  }
+}
+
+// asynchronous 16-byte copy global -> shared (completion per thread: the
+// thread that issued it waits and reads it)
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// the psi row of one node on one axis: CUT values from the fitted polynomial
+// rows in shared memory (the same rows for a whole warp) or the generic window
+template <int CUT>
+__device__ __forceinline__ void window_row(const WindowArgs &w, bool poly, const float *s_poly, int t, float dist,
+                                           float *v) {
+  constexpr int PS = LineGeom32<CUT>::PS;
+#pragma unroll
+  for (int c = 0; c < CUT; c++) {
+    if (poly && !(w.kind == WIN_BESSEL_I0 && c == 0 && dist == 0.f)) {
+      const float4 *rw = (const float4 *)(s_poly + (t * CUT + c) * PS);
+      v[c] = w.poly_ncoef <= 12 ? poly_horner12(rw[0], rw[1], rw[2], dist - 0.5f)
+                                : poly_horner(rw[0], rw[1], rw[2], rw[3], dist - 0.5f);
+    } else {
+      float out[3];
+      window_point<float>(w, t, c, dist, 0, out);
+      v[c] = out[0];
+    }
+  }
+}
+
+}  // namespace pg

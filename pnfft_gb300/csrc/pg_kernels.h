@@ -76,6 +76,7 @@ struct ConvArgs {
   int real_io;      // node arrays are real (c2r) instead of complex
   int accum;        // add into the node outputs (else store): ACCUMULATED, 2nd interlaced pass
   int generic;      // use the one-thread-per-node kernels (set per plan, e.g. by an autotuner)
+  int method;       // the plan's conv method (pnfft_gb300_set_conv_method)
   int64_t M;
   const double *x;  // [M][3]
   void *grid;       // n0*n1*n2 complex in compute precision, natural order
@@ -102,6 +103,8 @@ bool launch_interp_group(const ConvArgs &a, cudaStream_t s);
 // one warp per node on tile binnings (interp_tile_f32.cu, interp_tile_f64.cu)
 bool launch_interp_tile_f32(const ConvArgs &a, int mode, cudaStream_t s);
 bool launch_interp_tile_f64(const ConvArgs &a, int mode, cudaStream_t s);
+// FP32-mixed f-only spreading on a BIN_LINE binning (spread_line_f.cu)
+bool launch_spread_line_f(const ConvArgs &a, cudaStream_t s);
 // lines of tiles (spread_line_f32.cu, spread_line_f64.cu)
 bool launch_spread_line_f32(const ConvArgs &a, int mode, cudaStream_t s);
 bool launch_spread_line_f64(const ConvArgs &a, int mode, cudaStream_t s);
