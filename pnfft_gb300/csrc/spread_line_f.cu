@@ -26,7 +26,7 @@ namespace pg {
 // x row times f (complex) over the region's rows, and the y row over the
 // region's column pairs, zeros elsewhere.
 // ---------------------------------------------------------------------------
-constexpr int kFlushLineNodes = 256;
+constexpr int kFlushLineNodes = 64;
 
 template <int CUT>
 struct SpreadGeom32 {
