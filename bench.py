@@ -414,6 +414,7 @@ def run_gpu(args):
     if rank == 0 and world == 1 and not args.no_batch:
         line["batched"] = run_batched(P, torch, dev)
         line["particles"] = run_particles(P, torch, dev)
+        line["charge_dipole"] = run_charge_dipole(P)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(inputs=(x, fh, f))[0].items()
                                 if k != "seconds_per_step"}
@@ -543,6 +544,70 @@ def run_particles(P, torch, dev, steps=3):
     out["workload"] = ("c2r, N=64^3, n=128^3, M=2^21 (20% in 64 clusters, sigma 0.01), charges +-1, m=5; "
                        "step = adj + trafo(F|GRAD_F), FP32-mixed")
     return out
+
+
+def run_charge_dipole(P, steps=3):
+    """The charge/dipole sequence of the reference's particle test
+    (tests/check_charge_dipole.c:151-233), c2c, FP32-mixed: N = 64^3,
+    n = 128^3, Kaiser-Bessel m = 5, 2^20 charges and 2^18 dipoles uniform in
+    [-0.5, 0.5)^3, host node arrays.  One pnfft_gb300_charge_dipole call
+    (each node set copied and binned once, f_hat on the GPU throughout)
+    against the same four calls through pnfft_adj / pnfft_trafo.  Throughput
+    in particles per second; error of the energies against the FP64 call."""
+    import ctypes
+    from pnfft_gb300.particles import HostNodes, charge_dipole_host
+    L = P.load()
+    rng = np.random.default_rng(7)
+    N, m, Mc, Md = (64, 64, 64), 5, 1 << 20, 1 << 18
+    xc, xd = rng.uniform(-0.5, 0.5, (Mc, 3)), rng.uniform(-0.5, 0.5, (Md, 3))
+    q = rng.standard_normal(Mc) + 0j
+    mu = rng.standard_normal((Md, 3)) + 0j
+    out = {}
+    for prec in ("fp32", "fp64"):
+        p = P.Plan(N, m=m, precision=prec)
+        ch, di = HostNodes(Mc), HostNodes(Md)
+
+        def fill():
+            ch.x[:] = xc
+            ch.f[:] = q
+            di.x[:] = xd
+            di.grad_f[:] = mu
+
+        fill()
+        energy, _, _ = charge_dipole_host(p, ch, di)  # warm-up
+        fused = []
+        for _ in range(steps if prec == "fp32" else 1):
+            fill()
+            t0 = time.perf_counter()
+            energy, _, _ = charge_dipole_host(p, ch, di)
+            fused.append(time.perf_counter() - t0)
+        out[prec] = energy.copy()
+        if prec == "fp32":
+            fh = np.zeros(int(np.prod(N)), np.complex128)
+            L.pnfft_set_f_hat(fh.ctypes.data, p._p)
+            sep = []
+            for _ in range(steps + 1):
+                fill()
+                t0 = time.perf_counter()
+                L.pnfft_adj(p._p, ch.handle, P.COMPUTE_F)
+                buf = fh.copy()
+                L.pnfft_adj(p._p, di.handle, P.COMPUTE_GRAD_F)
+                fh += buf
+                L.pnfft_trafo(p._p, ch.handle, P.COMPUTE_F | P.COMPUTE_GRAD_F)
+                L.pnfft_trafo(p._p, di.handle, P.COMPUTE_GRAD_F | P.COMPUTE_HESSIAN_F)
+                sep.append(time.perf_counter() - t0)
+            sep = sep[1:]
+            t_fused = statistics.median(fused)
+            t_sep = statistics.median(sep)
+        ch.close()
+        di.close()
+        p.close()
+    err = float(np.linalg.norm(out["fp32"] - out["fp64"]) / np.linalg.norm(out["fp64"]))
+    return {"value": (Mc + Md) / t_fused / 1e6, "unit": "Mparticles/s", "ms_per_call": 1e3 * t_fused,
+            "four_calls_value": (Mc + Md) / t_sep / 1e6, "four_calls_ms": 1e3 * t_sep,
+            "err_energy_fp32_vs_fp64": err,
+            "workload": "c2c charge/dipole sequence, N=64^3, n=128^3, KB m=5, 2^20 charges + 2^18 dipoles, "
+                        "host arrays, FP32-mixed; energies and forces included"}
 
 
 def run_profile_case():

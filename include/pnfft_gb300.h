@@ -121,6 +121,23 @@ int pnfft_gb300_node_index(pnfft_plan ths, ptrdiff_t M, const double *x, int int
 int pnfft_gb300_sort_nodes_noalloc(const pnfft_plan ths, ptrdiff_t M, const double *d_x, long long *d_pairs,
                                    void *cuda_stream);
 
+/* The charge/dipole sequence of a particle-mesh code in one call; the
+ * reference runs it as four calls in tests/check_charge_dipole.c:151-233:
+ *   pnfft_adj(plan, charges, PNFFT_COMPUTE_F);
+ *   pnfft_adj(plan, dipoles, PNFFT_COMPUTE_GRAD_F);      (added to f_hat)
+ *   pnfft_trafo(plan, charges, PNFFT_COMPUTE_F | PNFFT_COMPUTE_GRAD_F);
+ *   pnfft_trafo(plan, dipoles, PNFFT_COMPUTE_GRAD_F | PNFFT_COMPUTE_HESSIAN_F);
+ * followed by the per-particle energies and forces.  Inputs: the charges in
+ * charges->f at charges->x, the dipole moments in dipoles->grad_f at
+ * dipoles->x (host arrays; a c2c plan).  On return the node arrays and the
+ * plan's f_hat hold what the four calls leave there, and, where not NULL,
+ * energy[Mc + Md] = (q phi, mu . grad phi) and force[3 (Mc + Md)] =
+ * (q grad phi, H mu).  Each node set is copied to the GPU and binned once for
+ * both of its transforms, and f_hat stays on the GPU between them.
+ * compute_flags may add PNFFT_OMIT_* flags.  Returns 0 on success. */
+int pnfft_gb300_charge_dipole(pnfft_plan ths, pnfft_nodes charges, pnfft_nodes dipoles, unsigned compute_flags,
+                              void *energy, void *force);
+
 /* Measurement aid, no counterpart in the reference: the FP32 multiply-add
  * rate of the current device in TFLOP/s (2 flops per multiply-add), timed with
  * CUDA events over a kernel of independent FMA chains on every SM: scalar

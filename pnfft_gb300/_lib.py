@@ -173,6 +173,7 @@ SIGNATURES = {
     "pnfft_gb300_sort_nodes_noalloc": (_I, [_P, _SS, _P, _P, _P]),
     "pnfft_gb300_last_stage_ms": (_I, [_P, _I, _DP]),
     "pnfft_gb300_measure_fp32_fma": (_I, [_I, _DP]),
+    "pnfft_gb300_charge_dipole": (_I, [_P, _P, _P, _U, _P, _P]),
 }
 
 _lib = None

@@ -16,6 +16,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <complex>
 #include <string>
 
 #include "pg_internal.h"
@@ -535,6 +536,56 @@ extern "C" void pnfft_adj(pnfft_plan ths, pnfft_nodes nodes, unsigned compute_fl
   if (ths == NULL) return;  // api-basic.c:350-351
   if (nodes == NULL && (~compute_flags & PNFFT_OMIT_CONV)) return;
   if (engine_adj(ths, nodes, compute_flags)) fprintf(stderr, "pnfft_adj: %s\n", last_error());
+}
+
+// The charge/dipole sequence of a particle-mesh code in one call, with the
+// per-particle energies and forces that the reference's particle test forms
+// after it (tests/check_charge_dipole.c:151-233): charges q = charges->f at
+// charges->x, dipole moments mu = dipoles->grad_f at dipoles->x.  On return
+// the node arrays hold what the four reference calls leave there (charges: f =
+// phi, grad_f = grad phi; dipoles: grad_f = grad phi, hessian_f = H), the plan's
+// f_hat holds the spectrum, and energy / force (Mc + Md and 3 (Mc + Md)
+// complex, may be NULL) hold q phi, q grad phi, mu . grad phi and H mu.
+extern "C" int pnfft_gb300_charge_dipole(pnfft_plan ths, pnfft_nodes charges, pnfft_nodes dipoles,
+                                         unsigned compute_flags, void *energy, void *force) {
+  if (!ths || !charges || !dipoles) {
+    set_error("pnfft_gb300_charge_dipole: plan and both node sets are required");
+    return -1;
+  }
+  if (ths->c2r) {
+    set_error("pnfft_gb300_charge_dipole: the sequence takes complex node values (a c2c plan)");
+    return -1;
+  }
+  const int64_t Mc = charges->local_M, Md = dipoles->local_M;
+  if ((Mc > 0 && (!charges->x || !charges->f || !charges->grad_f)) ||
+      (Md > 0 && (!dipoles->x || !dipoles->grad_f || !dipoles->hessian_f))) {
+    set_error("pnfft_gb300_charge_dipole: charges need x, f and grad_f; dipoles need x, grad_f and hessian_f");
+    return -1;
+  }
+  typedef std::complex<double> cd;
+  std::vector<cd> q(Mc), mu(3 * Md);
+  if (Mc) memcpy(q.data(), charges->f, sizeof(cd) * Mc);
+  if (Md) memcpy(mu.data(), dipoles->grad_f, sizeof(cd) * 3 * Md);
+  if (engine_charge_dipole(ths, charges, dipoles, compute_flags)) return -1;
+  const cd *phi = (const cd *)charges->f, *gc = (const cd *)charges->grad_f;
+  const cd *gd = (const cd *)dipoles->grad_f, *h = (const cd *)dipoles->hessian_f;
+  cd *en = (cd *)energy, *fo = (cd *)force;
+  for (int64_t j = 0; j < Mc; j++) {
+    if (en) en[j] = q[j] * phi[j];
+    if (fo)
+      for (int t = 0; t < 3; t++) fo[3 * j + t] = gc[3 * j + t] * q[j];
+  }
+  for (int64_t j = 0; j < Md; j++) {
+    const cd *m = &mu[3 * j], *g = gd + 3 * j, *H = h + 6 * j;  // xx, xy, xz, yy, yz, zz
+    if (en) en[Mc + j] = g[0] * m[0] + g[1] * m[1] + g[2] * m[2];
+    if (fo) {
+      cd *o = fo + 3 * (Mc + j);
+      o[0] = H[0] * m[0] + H[1] * m[1] + H[2] * m[2];
+      o[1] = H[1] * m[0] + H[3] * m[1] + H[4] * m[2];
+      o[2] = H[2] * m[0] + H[4] * m[1] + H[5] * m[2];
+    }
+  }
+  return 0;
 }
 
 extern "C" void pnfft_zero_f_hat(pnfft_plan ths) {  // api-basic.c:335-341

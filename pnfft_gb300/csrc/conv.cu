@@ -141,7 +141,7 @@ __global__ void __launch_bounds__(1024) k_bin_scan_b(Binning b, int *bsum, int n
     pa += x0;
     pb += x1;
   }
-  if (tid == 1023) *b.nsub = sb[1023];
+  if (tid == 1023) *(b.line_mode == BIN_LINE ? b.ntsub : b.nsub) = sb[1023];
 }
 
 __global__ void __launch_bounds__(256) k_bin_scan_c(Binning b, const int *bsum) {
@@ -215,14 +215,15 @@ __global__ void k_bin_scatter(int64_t M, Binning b, const void *__restrict__ rec
   }
 }
 
-__global__ void k_bin_subs(Binning b) {
+// runs of at most sub_max nodes of one key (tile), into the list (tile, first, cnt)
+__global__ void k_bin_subs(Binning b, int *tile, int *first, int *cntv) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= b.nkeys) return;
   int ns = b.nsub_tile[t], off = b.sub_off[t], st = b.start[t], c = b.count[t];
   for (int i = 0; i < ns; i++) {
-    b.sub_tile[off + i] = t;
-    b.sub_first[off + i] = st + i * b.sub_max;
-    b.sub_cnt[off + i] = min(b.sub_max, c - i * b.sub_max);
+    tile[off + i] = t;
+    first[off + i] = st + i * b.sub_max;
+    cntv[off + i] = min(b.sub_max, c - i * b.sub_max);
   }
 }
 
@@ -284,10 +285,11 @@ void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s) {
     const bool line = b.line_mode == BIN_LINE;
     const int group = line ? b.ntile[2] : kBlocksPerTile;
     const int nunits = line ? b.ntile[0] * b.ntile[1] : b.ntiles;
+    if (line) k_bin_subs<<<(b.nkeys + 255) / 256, 256, 0, s>>>(b, b.tsub_tile, b.tsub_first, b.tsub_cnt);
     cudaMemsetAsync(b.nsub, 0, 2 * sizeof(int), s);
     k_bin_group_subs<<<(nunits + 255) / 256, 256, 0, s>>>(b, a.M, group, nunits, 1);
   } else {
-    k_bin_subs<<<(b.nkeys + 255) / 256, 256, 0, s>>>(b);
+    k_bin_subs<<<(b.nkeys + 255) / 256, 256, 0, s>>>(b, b.sub_tile, b.sub_first, b.sub_cnt);
   }
 }
 
@@ -296,22 +298,24 @@ void bin_nodes(const ConvArgs &a, bool fp32, cudaStream_t s) {
 // ---------------------------------------------------------------------------
 void choose_tiles(int cut, bool fp32, bool spread, bool f_only, int method, const int *n, int64_t M, int *T,
                   int *line_mode) {
-  // Spreading, and the FP32-mixed interpolation of f alone (method 0): lines
-  // of 4x4x4-cell tiles along axis 2 (k_spread_line, k_interp_line; the
-  // record packs u2 in 15 bits).  Other interpolations: 8x8x8 cells per
-  // tile, the CTA stages the (8+2m)^3 region in shared memory (FP64, m=7:
-  // 170 KB).
+  // Lines of 4x4x4-cell tiles along axis 2 (the record packs u2 in 15 bits)
+  // for every kernel where the cutoff allows: the line kernels of B^T and of
+  // the FP32-mixed B of f, and the one-warp-per-node B over each 4x4x4 tile's
+  // (3+cutoff)^3 region for the other interpolations -- one binning serves both
+  // directions.  Conv methods 2 and 3 of the FP32-mixed B of f take 8x8x8
+  // tiles (one warp per node, or groups of nodes per warp).
   *line_mode = BIN_TILE;
-  const bool lines_fit = n[0] >= 4 && n[1] >= 4 && n[2] >= 4 && n[2] < 32768;
-  if (lines_fit && ((spread && cut <= 15) || (!spread && fp32 && f_only && method == 0 && cut <= 13))) {
+  const bool lines_fit = n[0] >= 4 && n[1] >= 4 && n[2] >= 4 && n[2] < 32768 && cut <= 15;
+  const bool tiles8 = !spread && fp32 && f_only && (method == 2 || method == 3);
+  if (lines_fit && !tiles8) {
     T[0] = T[1] = T[2] = 4;
     *line_mode = BIN_LINE;
     return;
   }
   for (int d = 0; d < 3; d++) T[d] = n[d] >= 8 ? 8 : n[d];
-  // method 3: the FP32-mixed interpolation groups the nodes of 2x2x4 corner
-  // blocks when there are enough of them (on average half a node per block
-  // or more); a group's z extent, cut + 3, must fit the 16 lanes of a half-warp
+  // method 3: groups of the nodes of 2x2x4 corner blocks when there are enough
+  // of them (on average half a node per block or more); a group's z extent,
+  // cut + 3, must fit the 16 lanes of a half-warp
   const int64_t ntiles = (int64_t)((n[0] + 7) / 8) * ((n[1] + 7) / 8) * ((n[2] + 7) / 8);
   if (!spread && fp32 && method == 3 && cut <= 13 && T[0] == 8 && T[1] == 8 && T[2] == 8 &&
       ntiles * kBlocksPerTile < (1 << 30) && 2 * M >= ntiles * kBlocksPerTile)
@@ -326,8 +330,19 @@ static bool tiles_usable(const ConvArgs &a) {
 
 int launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s) {
   if (a.M == 0) return CONV_NONE;
-  if (fp32 && mode == 1 && !a.generic && a.bin.line_mode == BIN_LINE && tiles_usable(a) && launch_interp_line(a, s))
+  if (fp32 && mode == 1 && a.method == 0 && a.bin.line_mode == BIN_LINE && tiles_usable(a) &&
+      launch_interp_line(a, s))
     return CONV_LINE;
+  if (!a.generic && a.bin.line_mode == BIN_LINE && tiles_usable(a)) {
+    // one warp per node over the 4x4x4 tiles of the line binning
+    ConvArgs t = a;
+    t.bin.sub_tile = a.bin.tsub_tile;
+    t.bin.sub_first = a.bin.tsub_first;
+    t.bin.sub_cnt = a.bin.tsub_cnt;
+    t.bin.nsub = a.bin.ntsub;
+    t.bin.max_subs = a.bin.max_tsubs;
+    if (fp32 ? launch_interp_tile_f32(t, mode, s) : launch_interp_tile_f64(t, mode, s)) return CONV_TILE;
+  }
   if (fp32 && mode == 1 && !a.generic && a.bin.line_mode == BIN_GROUP && tiles_usable(a) &&
       a.bin.sub_max <= kGroupSubMax && launch_interp_group(a, s))
     return CONV_GROUP;

@@ -67,20 +67,24 @@ struct DevState {
   uint64_t tables_for = ~0ull;
   double *fhat = nullptr;
   size_t fhat_cap = 0;
-  // node binnings [interpolation | spreading][plain | interlaced pass],
-  // allocated on first use; a valid binning of fixed nodes is reused
-  struct BinSlot {
-    Binning b = {};
-    int64_t cap = 0;
-    int T[3] = {0, 0, 0};
-    int line_mode = 0;
-    int prec = -1;
-    uint64_t uid = 0, ver = 0;
-    bool valid = false;
-  } bins[2][2];
   std::vector<Stage> pending;
   bool capturing = false;  // the current call is being captured into a CUDA graph
   std::vector<cudaEvent_t> free_ev;
+};
+
+// A binning of a node set onto grid tiles, kept with the node set: one slot
+// per layout (0: lines of 4x4x4 tiles, which serve B and B^T alike; 1: the
+// 8x8x8 tiles of conv methods 2 and 3) and interlacing pass.  A binning of
+// fixed nodes is reused by every later call with the same plan, precision and
+// coordinates, in either direction.
+struct BinSlot {
+  Binning b = {};
+  int64_t cap = 0;
+  int T[3] = {0, 0, 0};
+  int line_mode = 0;
+  int prec = -1;
+  uint64_t plan = 0, ver = 0;  // plan uid and node version of the binned nodes
+  bool valid = false;
 };
 
 struct NodeDev {
@@ -89,6 +93,7 @@ struct NodeDev {
   // the device copy of x matches the host x of this version (fixed nodes only)
   bool x_valid = false;
   uint64_t x_ver = 0;
+  BinSlot bins[2][2];  // [layout][plain | interlaced pass], allocated on first use
 };
 
 // ---------------------------------------------------------------------------
@@ -300,8 +305,9 @@ static int ensure_tables(pnfft_plan p) {
 }
 
 static void free_binning(Binning &b) {
-  int **arrs[] = {&b.key, &b.perm, &b.count, &b.start, &b.rank, &b.nsub_tile, &b.sub_off, &b.sub_tile,
-                  &b.sub_first, &b.sub_cnt, &b.nsub};
+  int **arrs[] = {&b.key,       &b.perm,    &b.count,    &b.start,      &b.rank,      &b.nsub_tile, &b.sub_off,
+                  &b.sub_tile,  &b.sub_first, &b.sub_cnt, &b.nsub,      &b.tsub_tile, &b.tsub_first, &b.tsub_cnt,
+                  &b.ntsub};
   for (int **a : arrs) {
     if (*a) cudaFree(*a);
     *a = nullptr;
@@ -313,17 +319,26 @@ static void free_binning(Binning &b) {
   b.bsum = nullptr;
 }
 
-static int ensure_binning(pnfft_plan p, int64_t M, int spread, int il, bool f_only) {
-  DevState *d = p->dev;
-  DevState::BinSlot &sl = d->bins[spread][il];
+static NodeDev *node_dev(pnfft_nodes nd) {
+  if (!nd->dev) nd->dev = new NodeDev();
+  return nd->dev;
+}
+
+// the binning slot of these nodes for pass `il` of a B (spread = 0) or B^T
+// (spread = 1), (re)allocated for the plan's tile shape when needed
+static BinSlot *ensure_binning(pnfft_plan p, pnfft_nodes nd, int spread, int il, bool f_only) {
+  const int64_t M = nd->local_M;
   int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
   int T[3], line_mode = 0;
   choose_tiles(p->cutoff, fp32(p), spread != 0, f_only, p->conv_method, n, M, T, &line_mode);
+  BinSlot &sl = node_dev(nd)->bins[line_mode == BIN_LINE ? 0 : 1][il];
   bool same = T[0] == sl.T[0] && T[1] == sl.T[1] && T[2] == sl.T[2] && line_mode == sl.line_mode;
-  if (same && sl.cap >= M && sl.b.key && sl.prec == p->precision) return 0;
+  for (int t = 0; t < 3; t++) same = same && sl.b.ntile[t] == (n[t] + T[t] - 1) / T[t];
+  if (same && sl.cap >= M && sl.b.key && sl.prec == p->precision) return &sl;
   int64_t cap = std::max<int64_t>(M, std::max<int64_t>(sl.cap, 1));
   Binning &b = sl.b;
   free_binning(b);
+  sl.valid = false;
   for (int t = 0; t < 3; t++) {
     b.T[t] = T[t];
     b.ntile[t] = (n[t] + T[t] - 1) / T[t];
@@ -334,26 +349,33 @@ static int ensure_binning(pnfft_plan p, int64_t M, int spread, int il, bool f_on
   b.sub_max = line_mode == BIN_LINE ? 2048 : 1024;
   const int units = line_mode == BIN_LINE ? b.ntile[0] * b.ntile[1] : b.ntiles;
   b.max_subs = (int)(units + cap / b.sub_max + 1);
-  PG_CUDA(cudaMalloc(&b.key, sizeof(int) * cap));
-  PG_CUDA(cudaMalloc(&b.perm, sizeof(int) * cap));
-  PG_CUDA(cudaMalloc(&b.count, sizeof(int) * b.nkeys));
-  PG_CUDA(cudaMalloc(&b.start, sizeof(int) * b.nkeys));
-  PG_CUDA(cudaMalloc(&b.rank, sizeof(int) * cap));
-  PG_CUDA(cudaMalloc(&b.nsub_tile, sizeof(int) * b.nkeys));
-  PG_CUDA(cudaMalloc(&b.sub_off, sizeof(int) * b.nkeys));
-  PG_CUDA(cudaMalloc(&b.sub_tile, sizeof(int) * b.max_subs));
-  PG_CUDA(cudaMalloc(&b.sub_first, sizeof(int) * b.max_subs));
-  PG_CUDA(cudaMalloc(&b.sub_cnt, sizeof(int) * b.max_subs));
-  PG_CUDA(cudaMalloc(&b.nsub, 2 * sizeof(int)));
-  PG_CUDA(cudaMalloc(&b.rec, (fp32(p) ? sizeof(float4) : sizeof(double4)) * cap));
-  PG_CUDA(cudaMalloc(&b.rec_tmp, (fp32(p) ? sizeof(float4) : sizeof(double4)) * cap));
-  PG_CUDA(cudaMalloc(&b.bsum, sizeof(int) * 2 * ((b.nkeys + 2047) / 2048 + 1)));
-  sl.valid = false;
+  b.max_tsubs = line_mode == BIN_LINE ? (int)(b.ntiles + cap / b.sub_max + 1) : 0;
+  auto alloc = [&](int **ptr, size_t count) -> bool {
+    if (cudaMalloc(ptr, sizeof(int) * std::max<size_t>(count, 1)) != cudaSuccess) {
+      set_error("device allocation of the node binning failed (%zu ints)", count);
+      return false;
+    }
+    return true;
+  };
+  const size_t recb = fp32(p) ? sizeof(float4) : sizeof(double4);
+  if (!alloc(&b.key, cap) || !alloc(&b.perm, cap) || !alloc(&b.count, b.nkeys) || !alloc(&b.start, b.nkeys) ||
+      !alloc(&b.rank, cap) || !alloc(&b.nsub_tile, b.nkeys) || !alloc(&b.sub_off, b.nkeys) ||
+      !alloc(&b.sub_tile, b.max_subs) || !alloc(&b.sub_first, b.max_subs) || !alloc(&b.sub_cnt, b.max_subs) ||
+      !alloc(&b.nsub, 2) || !alloc(&b.bsum, 2 * ((b.nkeys + 2047) / 2048 + 1)) ||
+      (line_mode == BIN_LINE && (!alloc(&b.tsub_tile, b.max_tsubs) || !alloc(&b.tsub_first, b.max_tsubs) ||
+                                 !alloc(&b.tsub_cnt, b.max_tsubs) || !alloc(&b.ntsub, 1))) ||
+      cudaMalloc(&b.rec, recb * cap) != cudaSuccess || cudaMalloc(&b.rec_tmp, recb * cap) != cudaSuccess) {
+    cudaGetLastError();
+    if (!last_error()[0]) set_error("device allocation of the node records failed");
+    free_binning(b);
+    sl.cap = 0;
+    return nullptr;
+  }
   sl.cap = cap;
   sl.prec = p->precision;
   sl.line_mode = line_mode;
   for (int t = 0; t < 3; t++) sl.T[t] = T[t];
-  return 0;
+  return &sl;
 }
 
 static int ensure_node_buffers(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
@@ -498,16 +520,16 @@ static int fft_exec(pnfft_plan p, int direction) {
 static int do_binning(pnfft_plan p, pnfft_nodes nd, ConvArgs &a, int il, int adj, cudaStream_t s, bool f_only) {
   DevState *d = p->dev;
   if (!s) s = d->stream;
-  if (ensure_binning(p, nd->local_M, adj, il, f_only)) return -1;
-  DevState::BinSlot &sl = d->bins[adj][il];
-  a.bin = sl.b;
-  bool reuse = nd->fixed && sl.valid && sl.uid == nd->uid && sl.ver == nd->version;
+  BinSlot *sl = ensure_binning(p, nd, adj, il, f_only);
+  if (!sl) return -1;
+  a.bin = sl->b;
+  const bool reuse = nd->fixed && sl->valid && sl->plan == p->uid && sl->ver == nd->version;
   if (!reuse) {
     StageScope sc(d, PNFFT_TIMER_SORT_NODES, adj, s);
     bin_nodes(a, fp32(p), s);
-    sl.valid = true;
-    sl.uid = nd->uid;
-    sl.ver = nd->version;
+    sl->valid = true;
+    sl->plan = p->uid;
+    sl->ver = nd->version;
   }
   return 0;
 }
@@ -953,6 +975,62 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
 }
 
 // ---------------------------------------------------------------------------
+// the charge/dipole sequence of a particle-mesh code in one call
+// (tests/check_charge_dipole.c:151-233 of the reference):
+//   f_hat = adj(charges, F) + adj(dipoles, GRAD_F);
+//   trafo(charges, F | GRAD_F);  trafo(dipoles, GRAD_F | HESSIAN_F)
+// with host arrays.  Both node sets are held fixed for the call (after one
+// version bump, so that their coordinates are read once more): each is
+// uploaded and binned once, and its binning serves its adjoint and its trafo
+// (both directions use the line binning).  f_hat stays on the device between
+// the transforms and is copied to the plan's f_hat at the end.
+// ---------------------------------------------------------------------------
+int engine_charge_dipole(pnfft_plan p, pnfft_nodes ch, pnfft_nodes di, unsigned cflags) {
+  if (ensure_dev(p)) return -1;
+  if (ch->u_x || di->u_x) {
+    set_error("pnfft_gb300_charge_dipole: the nodes carry device arrays; this call takes host arrays");
+    return -1;
+  }
+  if (p->d_f_hat_user) {
+    set_error("pnfft_gb300_charge_dipole: the plan carries a device f_hat; this call takes the host f_hat");
+    return -1;
+  }
+  DevState *d = p->dev;
+  const size_t fb = sizeof(double) * 2 * (size_t)p->local_N_total;
+  if (d->fhat_cap < fb) {
+    if (d->fhat) cudaFree(d->fhat);
+    d->fhat = nullptr;
+    d->fhat_cap = 0;
+    PG_CUDA(cudaMalloc(&d->fhat, fb > 0 ? fb : 16));
+    d->fhat_cap = fb;
+  }
+  const int fixed_ch = ch->fixed, fixed_di = di->fixed;
+  ch->version++;
+  di->version++;
+  ch->fixed = di->fixed = 1;
+  p->d_f_hat_user = d->fhat;
+  const unsigned extra = cflags & ~(PNFFT_COMPUTE_F | PNFFT_COMPUTE_GRAD_F | PNFFT_COMPUTE_HESSIAN_F |
+                                    PNFFT_COMPUTE_ACCUMULATED);
+  int rc = engine_adj(p, ch, extra | PNFFT_COMPUTE_F);
+  if (!rc) rc = engine_adj(p, di, extra | PNFFT_COMPUTE_GRAD_F | PNFFT_COMPUTE_ACCUMULATED);
+  if (!rc) rc = engine_trafo(p, ch, extra | PNFFT_COMPUTE_F | PNFFT_COMPUTE_GRAD_F);
+  if (!rc) rc = engine_trafo(p, di, extra | PNFFT_COMPUTE_GRAD_F | PNFFT_COMPUTE_HESSIAN_F);
+  p->d_f_hat_user = nullptr;
+  if (!rc && fb > 0 && p->f_hat) {
+    cudaError_t e = cudaMemcpyAsync(p->f_hat, d->fhat, fb, cudaMemcpyDeviceToHost, d->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
+    if (e != cudaSuccess) {
+      set_error("pnfft_gb300_charge_dipole: copying f_hat back failed: %s", cudaGetErrorString(e));
+      rc = -1;
+    }
+  }
+  ch->fixed = fixed_ch;
+  di->fixed = fixed_di;
+  engine_flush_timers(p);
+  return rc;
+}
+
+// ---------------------------------------------------------------------------
 // misc
 // ---------------------------------------------------------------------------
 int engine_set_stream(pnfft_plan p, void *stream) {
@@ -986,8 +1064,6 @@ void engine_release_plan(pnfft_plan p) {
         if (d->tab[a][t]) cudaFree(d->tab[a][t]);
     if (d->fhat) cudaFree(d->fhat);
     if (d->poly) cudaFree(d->poly);
-    for (auto &row : d->bins)
-      for (auto &sl : row) free_binning(sl.b);
     for (cudaEvent_t e : d->free_ev) cudaEventDestroy(e);
     if (d->own) cudaStreamDestroy(d->own);
     if (d->aux) cudaStreamDestroy(d->aux);
@@ -1006,6 +1082,8 @@ void engine_release_nodes(pnfft_nodes nd) {
   cudaFree(v->f);
   cudaFree(v->grad);
   cudaFree(v->hess);
+  for (auto &row : v->bins)
+    for (auto &sl : row) free_binning(sl.b);
   cudaGetLastError();
   delete v;
   nd->dev = nullptr;

@@ -16,19 +16,21 @@
 namespace pg {
 
 // ---------------------------------------------------------------------------
-// interpolation B, tiled.  The CTA stages its tile's (8+2m)^3 region in
-// shared memory, then walks its nodes in batches: (1) all threads evaluate
+// interpolation B, tiled.  The CTA stages its tile's (TE+2m)^3 region in
+// shared memory (TE = 4: a tile of a line binning, whose records carry the
+// full lowest z index; TE = 8: an 8x8x8-cell tile binning), then walks its
+// nodes in batches: (1) all threads evaluate
 // the window values of the batch (3 x cutoff per node and derivative), (2)
 // one warp per node sums the 13^3 stencil -- lanes (row = lane/16, col =
 // lane%16) read two z-rows of 13 consecutive grid values per step, with the
 // x-window in registers -- and reduces with shuffles, (3) the batch's results
 // are converted and written by all threads.
 // ---------------------------------------------------------------------------
-template <typename T, int CUT, int MODE>
+template <typename T, int CUT, int MODE, int TE>
 struct InterpGeom {
   static constexpr bool DF = (MODE & 1) != 0, DG = (MODE & 2) != 0, DH = (MODE & 4) != 0;
   static constexpr int NDER = DH ? 2 : (DG ? 1 : 0);
-  static constexpr int R = 8 + CUT - 1, PL = R * R, VOL = R * R * R;
+  static constexpr int R = TE + CUT - 1, PL = R * R, VOL = R * R * R;
   static constexpr int NV = 3 * CUT * (NDER + 1);
   static constexpr int NC = (DF ? 1 : 0) + (DG ? 3 : 0) + (DH ? 6 : 0);
   static constexpr int NBI = sizeof(T) == 4 ? 48 : 32;
@@ -36,10 +38,10 @@ struct InterpGeom {
                                  (size_t)NBI * 2 * sizeof(int);
 };
 
-template <typename T, int CUT, int MODE>
+template <typename T, int CUT, int MODE, int TE>
 __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
   typedef typename Cplx<T>::type C;
-  typedef InterpGeom<T, CUT, MODE> G;
+  typedef InterpGeom<T, CUT, MODE, TE> G;
   constexpr bool DF = G::DF, DG = G::DG, DH = G::DH;
   constexpr int NDER = G::NDER, R = G::R, PL = G::PL, VOL = G::VOL, NV = G::NV, NC = G::NC, NBI = G::NBI;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -96,6 +98,7 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
       const T *wv = s_w + i * NV;
       int o[3];
       unpack_corner(s_o[i], o);
+      if (TE == 4) o[2] = ((s_o[i] >> 16) & 0x7fff) - base[2];  // line records: the full u2
       T px[CUT], dpx[CUT], ddpx[CUT];
 #pragma unroll
       for (int l = 0; l < CUT; l++) {
@@ -216,41 +219,48 @@ __global__ void __launch_bounds__(256) k_interp_tile(ConvArgs a) {
   }
 }
 
-template <typename T, int CUT, int MODE>
+template <typename T, int CUT, int MODE, int TE>
 static void run_interp_tile(const ConvArgs &a, cudaStream_t s) {
-  const size_t sm = InterpGeom<T, CUT, MODE>::SMEM;
+  const size_t sm = InterpGeom<T, CUT, MODE, TE>::SMEM;
   // the shared-memory opt-in is a per-device attribute of the kernel
   static std::atomic<unsigned long long> attr_done{0};
   int dev = 0;
   cudaGetDevice(&dev);
   const unsigned long long bit = 1ull << (dev & 63);
   if (!(attr_done.load() & bit)) {
-    cudaFuncSetAttribute(k_interp_tile<T, CUT, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaFuncSetAttribute(k_interp_tile<T, CUT, MODE, TE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     attr_done.fetch_or(bit);
   }
-  k_interp_tile<T, CUT, MODE><<<a.bin.max_subs, 256, sm, s>>>(a);
+  k_interp_tile<T, CUT, MODE, TE><<<a.bin.max_subs, 256, sm, s>>>(a);
 }
 
-template <typename T, int MODE>
+template <typename T, int MODE, int TE>
 static bool interp_tile_by_cut(const ConvArgs &a, cudaStream_t s) {
   switch (a.w.cut) {
-    case 5: run_interp_tile<T, 5, MODE>(a, s); return true;
-    case 7: run_interp_tile<T, 7, MODE>(a, s); return true;
-    case 9: run_interp_tile<T, 9, MODE>(a, s); return true;
-    case 11: run_interp_tile<T, 11, MODE>(a, s); return true;
-    case 13: run_interp_tile<T, 13, MODE>(a, s); return true;
-    case 15: run_interp_tile<T, 15, MODE>(a, s); return true;
+    case 5: run_interp_tile<T, 5, MODE, TE>(a, s); return true;
+    case 7: run_interp_tile<T, 7, MODE, TE>(a, s); return true;
+    case 9: run_interp_tile<T, 9, MODE, TE>(a, s); return true;
+    case 11: run_interp_tile<T, 11, MODE, TE>(a, s); return true;
+    case 13: run_interp_tile<T, 13, MODE, TE>(a, s); return true;
+    case 15: run_interp_tile<T, 15, MODE, TE>(a, s); return true;
     default: return false;
   }
 }
 
+// 4x4x4 tiles of a line binning in every mode; 8x8x8 tiles only for the
+// FP32-mixed f (conv methods 2 and 3)
 template <typename T>
 static bool interp_tile_t(const ConvArgs &a, int mode, cudaStream_t s) {
+  if (a.bin.T[0] == 8) {
+    if (sizeof(T) == 4 && mode == 1) return interp_tile_by_cut<T, 1, 8>(a, s);
+    return false;
+  }
+  if (a.bin.T[0] != 4) return false;
   switch (mode) {
-    case 1: return interp_tile_by_cut<T, 1>(a, s);
-    case 2: return interp_tile_by_cut<T, 2>(a, s);
-    case 3: return interp_tile_by_cut<T, 3>(a, s);
-    case 4: return interp_tile_by_cut<T, 4>(a, s);
+    case 1: return interp_tile_by_cut<T, 1, 4>(a, s);
+    case 2: return interp_tile_by_cut<T, 2, 4>(a, s);
+    case 3: return interp_tile_by_cut<T, 3, 4>(a, s);
+    case 4: return interp_tile_by_cut<T, 4, 4>(a, s);
     default: return false;
   }
 }

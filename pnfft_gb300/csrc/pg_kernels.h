@@ -33,7 +33,9 @@ constexpr int kPolyCoef = 16;
 // tile; one CTA handles one sub-problem.  In line mode a sub-problem is a run
 // of the nodes of one line of tiles along axis 2 (the tiles with the same
 // t0, t1, which the sort keeps consecutive and in slab order), and the
-// records carry the full lowest z index u2 instead of the in-tile offset.
+// records carry the full lowest z index u2 instead of the in-tile offset; a
+// second list cuts the same sorted nodes by tile, so that every kernel can run
+// on a line binning and one binning serves both directions.
 // In group mode (FP32-mixed interpolation, conv method 3) the sort key is finer: the tile
 // and the 2x2x4 block of stencil corners within it (32 keys per tile), and
 // the record of every kGroupMax-th node of a block (by rank) carries a
@@ -48,6 +50,7 @@ constexpr int kGroupSubMax = 1024;  // nodes per sub-problem of the grouped inte
 struct Binning {
   int T[3], ntile[3];
   int ntiles, sub_max, max_subs;
+  int max_tsubs;   // line mode: capacity of the tile sub-problem list below
   int line_mode;   // BinMode
   int nkeys;       // sort keys: ntiles, or ntiles * kBlocksPerTile in group mode
   int *key;        // [M] sort key of each node
@@ -61,6 +64,10 @@ struct Binning {
   int *sub_first;  // [max_subs]
   int *sub_cnt;    // [max_subs]
   int *nsub;       // [2] sub-problem count; [1]: runs beyond the first per unit (group mode)
+  // line mode: the same sorted nodes cut into runs of one 4x4x4 tile (at most
+  // sub_max nodes each), for the one-warp-per-node interpolation kernels
+  int *tsub_tile, *tsub_first, *tsub_cnt;  // [max_tsubs]
+  int *ntsub;                              // [1]
   void *rec;       // [M] node records in tile order: float4 (FP32-mixed) or double4
                    // {dist0, dist1, dist2, local stencil corner o0 | o1<<8 | o2<<16}
   void *rec_tmp;   // [M] the same records in node order (before the scatter)

@@ -16,17 +16,78 @@ Here the same sequence runs on torch CUDA tensors through the C ABI:
 - the second adjoint accumulates into f_hat with COMPUTE_ACCUMULATED, where
   the reference copies f_hat into a buffer and adds it back;
 - one plan serves both node sets, as in the reference; each call bins its
-  node set (the binning cache of a plan holds one node set per direction).
+  node set, unless the set is fixed (pnfft_gb300_nodes_set_fixed): a node
+  set keeps its binning, which serves both directions.
+
+``charge_dipole_host`` runs the whole sequence on host arrays through one C
+call, pnfft_gb300_charge_dipole: each node set is copied to the GPU and
+binned once for both of its transforms, and f_hat stays on the GPU.
 
 ``charges_c2r`` is the real-valued charge-only form: adj(q), then trafo
 with the gradient, either analytic or ik-differentiated (PNFFT_DIFF_IK on
 the plan).
 """
+import ctypes
+
+import numpy as np
 import torch
 
-from . import COMPUTE_ACCUMULATED, COMPUTE_F, COMPUTE_GRAD_F, COMPUTE_HESSIAN_F
+from . import COMPUTE_ACCUMULATED, COMPUTE_F, COMPUTE_GRAD_F, COMPUTE_HESSIAN_F, _check, load
+from ._lib import MALLOC_F, MALLOC_GRAD_F, MALLOC_HESSIAN_F, MALLOC_X
 
-__all__ = ["charge_dipole", "charges_c2r"]
+__all__ = ["charge_dipole", "charge_dipole_host", "charges_c2r", "HostNodes"]
+
+
+class HostNodes:
+    """A pnfft_nodes object of M nodes owning page-locked host arrays x, f,
+    grad_f and hessian_f (PNFFT_MALLOC_*), with numpy views of them."""
+
+    def __init__(self, M):
+        L = load()
+        self.M = int(M)
+        flags = MALLOC_X | MALLOC_F | MALLOC_GRAD_F | MALLOC_HESSIAN_F
+        self.handle = L.pnfft_init_nodes(self.M, ctypes.c_uint(flags))
+        dp = ctypes.POINTER(ctypes.c_double)
+
+        def view(ptr, n):
+            return np.ctypeslib.as_array(ctypes.cast(ptr, dp), (n,)) if self.M else np.zeros(n)
+
+        self.x = view(L.pnfft_get_x(self.handle), 3 * self.M).reshape(-1, 3)
+        self.f = view(L.pnfft_get_f(self.handle), 2 * self.M).view(np.complex128)
+        self.grad_f = view(L.pnfft_get_grad_f(self.handle), 6 * self.M).view(np.complex128).reshape(-1, 3)
+        self.hessian_f = view(L.pnfft_get_hessian_f(self.handle), 12 * self.M).view(np.complex128).reshape(-1, 6)
+
+    def close(self):
+        if self.handle:
+            load().pnfft_free_nodes(self.handle, ctypes.c_uint(0xF))
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def charge_dipole_host(plan, charges, dipoles, compute_flags=0):
+    """The sequence of charge_dipole on HostNodes through pnfft_gb300_charge_dipole.
+
+    charges.f holds the charges, dipoles.grad_f the dipole moments.  Returns
+    (energy, force, f_hat): energy (Mc + Md,) and force (Mc + Md, 3) complex;
+    the node arrays hold phi / grad phi (charges) and grad phi / H (dipoles).
+    """
+    L = load()
+    M = charges.M + dipoles.M
+    energy = np.zeros(M, np.complex128)
+    force = np.zeros((M, 3), np.complex128)
+    S = int(np.prod(plan.local_N))
+    f_hat = np.zeros(S, np.complex128)
+    L.pnfft_set_f_hat(f_hat.ctypes.data, plan._p)
+    L.pnfft_gb300_clear_error()
+    rc = L.pnfft_gb300_charge_dipole(plan._p, charges.handle, dipoles.handle, ctypes.c_uint(compute_flags),
+                                     energy.ctypes.data, force.ctypes.data)
+    _check(rc, "pnfft_gb300_charge_dipole")
+    return energy, force, f_hat
 
 
 def charge_dipole(plan, xc, q, xd, mu):

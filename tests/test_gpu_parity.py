@@ -362,3 +362,84 @@ def test_fp32_tables_fraction_rounding_to_one(gpu, oracle, table):
     o = oracle.OraclePlan(N, n, m=m, flags=flags)
     assert rel(p.adj(x, f), o.adj(x, f)) < FP32_TOL
     assert rel(p.trafo(x, fh)[0], o.trafo(x, fh)[0]) < FP32_TOL
+
+
+def test_fp64_vs_reference_fixtures(gpu):
+    # outputs of the reference's own C code (tests/golden/ref_golden.npz, made
+    # by tests/golden/make_ref_golden.py from oracle/_ref): FP64 to 1e-12
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_golden.npz"))
+    for case in sorted({k.split("/")[0] for k in d.files}):
+        N, n = tuple(int(v) for v in d[case + "/N"]), tuple(int(v) for v in d[case + "/n"])
+        m, flags, cf = int(d[case + "/m"]), int(d[case + "/flags"]), int(d[case + "/cflags"])
+        p = gpu.Plan(N, n, m=m, flags=flags)
+        x, fh, f, g = d[case + "/x"], d[case + "/f_hat"], d[case + "/f"], d[case + "/grad"]
+        got = p.trafo(x, fh, cf)
+        keys = [k.split("/")[1] for k in d.files if k.startswith(case + "/")]
+        for name, a in zip(("trafo_f", "trafo_grad", "trafo_hess"), got):
+            if name in keys:
+                assert rel(a, d[case + "/" + name]) < FP64_TOL, (case, name)
+        assert rel(p.adj(x, f, g, 1 | 2), d[case + "/adj"]) < FP64_TOL, case
+        p.close()
+
+
+def _c_arrays(L, nd, M):
+    import ctypes
+    dp = ctypes.POINTER(ctypes.c_double)
+    x = np.ctypeslib.as_array(ctypes.cast(L.pnfft_get_x(nd), dp), (3 * M,))
+    f = np.ctypeslib.as_array(ctypes.cast(L.pnfft_get_f(nd), dp), (2 * M,))
+    return x, f
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL)])
+def test_precompute_psi_through_the_c_abi(gpu, oracle, prec, tol):
+    # the reference caller sequence: pnfft_init_nodes, pnfft_precompute_psi
+    # (PNFFT_PRE_PSI), pnfft_trafo / pnfft_adj; then the coordinates change in
+    # place and pnfft_precompute_psi is called again, as the reference asks
+    # (ndft-parallel.c:1144): the results follow the new coordinates
+    import ctypes
+    L = gpu.load()
+    N, n, m, M = (16, 16, 16), (32, 32, 32), 5, 2000
+    Nc, nc = (ctypes.c_ssize_t * 3)(*N), (ctypes.c_ssize_t * 3)(*n)
+    xm = (ctypes.c_double * 3)(0.5, 0.5, 0.5)
+    flags = gpu.MALLOC_F_HAT | (gpu.GB300_FP32 if prec == "fp32" else 0)
+    p = L.pnfft_init_guru(3, Nc, nc, xm, m, ctypes.c_uint(flags), gpu.PFFT_ESTIMATE, gpu.MPI_COMM_WORLD)
+    nd = L.pnfft_init_nodes(M, gpu.MALLOC_X | gpu.MALLOC_F)
+    hx, hf = _c_arrays(L, nd, M)
+    hfh = np.ctypeslib.as_array(ctypes.cast(L.pnfft_get_f_hat(p), ctypes.POINTER(ctypes.c_double)), (2 * 4096,))
+    o = oracle.OraclePlan(N, n, m=m)
+    rng = np.random.default_rng(51)
+    fh = rng.standard_normal(4096) + 1j * rng.standard_normal(4096)
+    for rep in range(2):
+        x = rng.uniform(-0.5, 0.5, (M, 3))
+        hx[:] = x.ravel()  # in place: the same array, new coordinates
+        L.pnfft_precompute_psi(p, nd, gpu.PRE_PSI)
+        for _ in range(2):  # the second call reuses the fixed nodes' binning
+            hfh[:] = fh.view(np.float64)
+            L.pnfft_trafo(p, nd, gpu.COMPUTE_F)
+            assert rel(hf.view(np.complex128), o.trafo(x, fh)[0]) < tol, rep
+        f = rng.standard_normal(M) + 1j * rng.standard_normal(M)
+        hf[:] = f.view(np.float64)
+        L.pnfft_adj(p, nd, gpu.COMPUTE_F)
+        assert rel(hfh.view(np.complex128), o.adj(x, f)) < tol, rep
+    L.pnfft_free_nodes(nd, gpu.FREE_X | gpu.FREE_F)
+    L.pnfft_finalize(p, gpu.FREE_F_HAT)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", FP64_TOL), ("fp32", FP32_TOL)])
+def test_x_max_below_half(gpu, oracle, prec, tol):
+    # x_max < 0.5: the reference prunes its FFT output to the grid points the
+    # nodes reach (api-guru.c:195-218); here the whole grid is kept, which gives
+    # the same values for nodes in [-x_max, x_max)
+    N, n, m = (16, 16, 16), (32, 32, 32), 4
+    xmax = np.array([0.25, 0.5, 0.125])
+    rng = np.random.default_rng(52)
+    x = rng.uniform(-1, 1, (1500, 3)) * xmax
+    fh = rng.standard_normal(4096) + 1j * rng.standard_normal(4096)
+    f = rng.standard_normal(1500) + 1j * rng.standard_normal(1500)
+    p = gpu.Plan(N, n, m=m, x_max=xmax, precision=prec)
+    assert p.lower_border == tuple(-xmax) and p.upper_border == tuple(xmax)
+    o = oracle.OraclePlan(N, n, m=m)
+    for a, b in zip(p.trafo(x, fh, 1 | 2), o.trafo(x, fh, 1 | 2)):
+        assert rel(a, b) < tol
+    assert rel(p.adj(x, f), o.adj(x, f)) < tol
