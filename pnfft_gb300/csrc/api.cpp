@@ -16,7 +16,6 @@
 #include <string.h>
 
 #include <atomic>
-#include <complex>
 #include <string>
 
 #include "pg_internal.h"
@@ -562,30 +561,7 @@ extern "C" int pnfft_gb300_charge_dipole(pnfft_plan ths, pnfft_nodes charges, pn
     set_error("pnfft_gb300_charge_dipole: charges need x, f and grad_f; dipoles need x, grad_f and hessian_f");
     return -1;
   }
-  typedef std::complex<double> cd;
-  std::vector<cd> q(Mc), mu(3 * Md);
-  if (Mc) memcpy(q.data(), charges->f, sizeof(cd) * Mc);
-  if (Md) memcpy(mu.data(), dipoles->grad_f, sizeof(cd) * 3 * Md);
-  if (engine_charge_dipole(ths, charges, dipoles, compute_flags)) return -1;
-  const cd *phi = (const cd *)charges->f, *gc = (const cd *)charges->grad_f;
-  const cd *gd = (const cd *)dipoles->grad_f, *h = (const cd *)dipoles->hessian_f;
-  cd *en = (cd *)energy, *fo = (cd *)force;
-  for (int64_t j = 0; j < Mc; j++) {
-    if (en) en[j] = q[j] * phi[j];
-    if (fo)
-      for (int t = 0; t < 3; t++) fo[3 * j + t] = gc[3 * j + t] * q[j];
-  }
-  for (int64_t j = 0; j < Md; j++) {
-    const cd *m = &mu[3 * j], *g = gd + 3 * j, *H = h + 6 * j;  // xx, xy, xz, yy, yz, zz
-    if (en) en[Mc + j] = g[0] * m[0] + g[1] * m[1] + g[2] * m[2];
-    if (fo) {
-      cd *o = fo + 3 * (Mc + j);
-      o[0] = H[0] * m[0] + H[1] * m[1] + H[2] * m[2];
-      o[1] = H[1] * m[0] + H[3] * m[1] + H[4] * m[2];
-      o[2] = H[2] * m[0] + H[4] * m[1] + H[5] * m[2];
-    }
-  }
-  return 0;
+  return engine_charge_dipole(ths, charges, dipoles, compute_flags, energy, force);
 }
 
 extern "C" void pnfft_zero_f_hat(pnfft_plan ths) {  // api-basic.c:335-341

@@ -3,6 +3,7 @@
 // pnfft_trafo) and spreading B^T (nodes -> grid, pnfft_adj) to the kernels:
 //   * interp_line.cu: FP32-mixed B (f only) over lines of tiles with
 //     register-resident grid columns (the transpose of the spreading);
+//   * interp_line_g.cu: the same with the gradient (FP32-mixed);
 //   * interp_group.cu: FP32-mixed B (f only), groups of nodes per warp;
 //   * interp_tile.cuh (interp_tile_f32.cu, interp_tile_f64.cu): B, one warp
 //     per node over a shared-memory copy of the tile's region;
@@ -332,6 +333,9 @@ int launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s) {
   if (a.M == 0) return CONV_NONE;
   if (fp32 && mode == 1 && a.method == 0 && a.bin.line_mode == BIN_LINE && tiles_usable(a) &&
       launch_interp_line(a, s))
+    return CONV_LINE;
+  if (fp32 && (mode == 2 || mode == 3) && a.method == 0 && a.bin.line_mode == BIN_LINE && tiles_usable(a) &&
+      a.w.cut <= 13 && launch_interp_line_g(a, mode, s))
     return CONV_LINE;
   if (!a.generic && a.bin.line_mode == BIN_LINE && tiles_usable(a)) {
     // one warp per node over the 4x4x4 tiles of the line binning

@@ -985,7 +985,31 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
 // (both directions use the line binning).  f_hat stays on the device between
 // the transforms and is copied to the plan's f_hat at the end.
 // ---------------------------------------------------------------------------
-int engine_charge_dipole(pnfft_plan p, pnfft_nodes ch, pnfft_nodes di, unsigned cflags) {
+// energy and force of each particle: charges q phi and q grad phi, dipoles
+// mu . grad phi and H mu (H in the order xx, xy, xz, yy, yz, zz)
+__global__ void k_charge_dipole_results(int64_t Mc, int64_t Md, const double2 *__restrict__ q,
+                                        const double2 *__restrict__ phi, const double2 *__restrict__ gc,
+                                        const double2 *__restrict__ mu, const double2 *__restrict__ gd,
+                                        const double2 *__restrict__ h, double2 *__restrict__ energy,
+                                        double2 *__restrict__ force) {
+  const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  auto mul = [](double2 a, double2 b) { return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
+  auto add = [](double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); };
+  if (j < Mc) {
+    energy[j] = mul(q[j], phi[j]);
+    for (int t = 0; t < 3; t++) force[3 * j + t] = mul(gc[3 * j + t], q[j]);
+  } else if (j < Mc + Md) {
+    const int64_t k = j - Mc;
+    const double2 *m = mu + 3 * k, *g = gd + 3 * k, *H = h + 6 * k;
+    energy[j] = add(add(mul(g[0], m[0]), mul(g[1], m[1])), mul(g[2], m[2]));
+    double2 *o = force + 3 * j;
+    o[0] = add(add(mul(H[0], m[0]), mul(H[1], m[1])), mul(H[2], m[2]));
+    o[1] = add(add(mul(H[1], m[0]), mul(H[3], m[1])), mul(H[4], m[2]));
+    o[2] = add(add(mul(H[2], m[0]), mul(H[4], m[1])), mul(H[5], m[2]));
+  }
+}
+
+int engine_charge_dipole(pnfft_plan p, pnfft_nodes ch, pnfft_nodes di, unsigned cflags, void *energy, void *force) {
   if (ensure_dev(p)) return -1;
   if (ch->u_x || di->u_x) {
     set_error("pnfft_gb300_charge_dipole: the nodes carry device arrays; this call takes host arrays");
@@ -996,6 +1020,8 @@ int engine_charge_dipole(pnfft_plan p, pnfft_nodes ch, pnfft_nodes di, unsigned 
     return -1;
   }
   DevState *d = p->dev;
+  cudaStream_t s = d->stream;
+  const int64_t Mc = ch->local_M, Md = di->local_M;
   const size_t fb = sizeof(double) * 2 * (size_t)p->local_N_total;
   if (d->fhat_cap < fb) {
     if (d->fhat) cudaFree(d->fhat);
@@ -1004,6 +1030,11 @@ int engine_charge_dipole(pnfft_plan p, pnfft_nodes ch, pnfft_nodes di, unsigned 
     PG_CUDA(cudaMalloc(&d->fhat, fb > 0 ? fb : 16));
     d->fhat_cap = fb;
   }
+  // q (Mc), mu (3 Md), energy (Mc + Md), force (3 (Mc + Md)) on the device
+  double2 *buf = nullptr;
+  const size_t nbuf = (size_t)(Mc + 3 * Md + 4 * (Mc + Md));
+  PG_CUDA(cudaMallocAsync(&buf, sizeof(double2) * std::max<size_t>(nbuf, 1), s));
+  double2 *q = buf, *mu = q + Mc, *en = mu + 3 * Md, *fo = en + (Mc + Md);
   const int fixed_ch = ch->fixed, fixed_di = di->fixed;
   ch->version++;
   di->version++;
@@ -1011,21 +1042,50 @@ int engine_charge_dipole(pnfft_plan p, pnfft_nodes ch, pnfft_nodes di, unsigned 
   p->d_f_hat_user = d->fhat;
   const unsigned extra = cflags & ~(PNFFT_COMPUTE_F | PNFFT_COMPUTE_GRAD_F | PNFFT_COMPUTE_HESSIAN_F |
                                     PNFFT_COMPUTE_ACCUMULATED);
+  auto keep = [&](double2 *dst, const double *src, int64_t count) -> int {  // device copy of an input
+    if (count > 0 && cudaMemcpyAsync(dst, src, sizeof(double2) * count, cudaMemcpyDeviceToDevice, s) != cudaSuccess) {
+      set_error("pnfft_gb300_charge_dipole: keeping the inputs failed");
+      return -1;
+    }
+    return 0;
+  };
   int rc = engine_adj(p, ch, extra | PNFFT_COMPUTE_F);
+  if (!rc && Mc > 0) rc = keep(q, ch->dev->f, Mc);  // uploaded by the adjoint
   if (!rc) rc = engine_adj(p, di, extra | PNFFT_COMPUTE_GRAD_F | PNFFT_COMPUTE_ACCUMULATED);
+  if (!rc && Md > 0) rc = keep(mu, di->dev->grad, 3 * Md);
   if (!rc) rc = engine_trafo(p, ch, extra | PNFFT_COMPUTE_F | PNFFT_COMPUTE_GRAD_F);
   if (!rc) rc = engine_trafo(p, di, extra | PNFFT_COMPUTE_GRAD_F | PNFFT_COMPUTE_HESSIAN_F);
   p->d_f_hat_user = nullptr;
+  ch->fixed = fixed_ch;
+  di->fixed = fixed_di;
+  if (!rc && (energy || force) && Mc + Md > 0) {
+    const double2 *none = nullptr;
+    k_charge_dipole_results<<<(unsigned)((Mc + Md + 255) / 256), 256, 0, s>>>(
+        Mc, Md, q, Mc ? (const double2 *)ch->dev->f : none, Mc ? (const double2 *)ch->dev->grad : none, mu,
+        Md ? (const double2 *)di->dev->grad : none, Md ? (const double2 *)di->dev->hess : none, en, fo);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && energy)
+      e = cudaMemcpyAsync(energy, en, sizeof(double2) * (Mc + Md), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && force)
+      e = cudaMemcpyAsync(force, fo, sizeof(double2) * 3 * (Mc + Md), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) {
+      set_error("pnfft_gb300_charge_dipole: the energies and forces failed: %s", cudaGetErrorString(e));
+      rc = -1;
+    }
+  }
   if (!rc && fb > 0 && p->f_hat) {
-    cudaError_t e = cudaMemcpyAsync(p->f_hat, d->fhat, fb, cudaMemcpyDeviceToHost, d->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(d->stream);
+    cudaError_t e = cudaMemcpyAsync(p->f_hat, d->fhat, fb, cudaMemcpyDeviceToHost, s);
     if (e != cudaSuccess) {
       set_error("pnfft_gb300_charge_dipole: copying f_hat back failed: %s", cudaGetErrorString(e));
       rc = -1;
     }
   }
-  ch->fixed = fixed_ch;
-  di->fixed = fixed_di;
+  cudaFreeAsync(buf, s);
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (!rc && e != cudaSuccess) {
+    set_error("pnfft_gb300_charge_dipole: %s", cudaGetErrorString(e));
+    rc = -1;
+  }
   engine_flush_timers(p);
   return rc;
 }

@@ -71,7 +71,8 @@ const char *last_error();
 // engine.cu
 int engine_trafo(pnfft_plan ths, pnfft_nodes nodes, unsigned cflags);
 int engine_adj(pnfft_plan ths, pnfft_nodes nodes, unsigned cflags);
-int engine_charge_dipole(pnfft_plan ths, pnfft_nodes charges, pnfft_nodes dipoles, unsigned cflags);
+int engine_charge_dipole(pnfft_plan ths, pnfft_nodes charges, pnfft_nodes dipoles, unsigned cflags, void *energy,
+                         void *force);
 int engine_set_stream(pnfft_plan ths, void *stream);
 int engine_sync(pnfft_plan ths);
 void engine_release_plan(pnfft_plan ths);

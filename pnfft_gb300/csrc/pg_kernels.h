@@ -105,6 +105,8 @@ int launch_spread(const ConvArgs &a, int mode, bool fp32, cudaStream_t s);
 // when it has no instance for the cutoff or mode.
 // FP32-mixed f-only interpolation on a BIN_LINE binning (interp_line.cu)
 bool launch_interp_line(const ConvArgs &a, cudaStream_t s);
+// FP32-mixed interpolation with the gradient (mode 2 or 3) on a BIN_LINE binning (interp_line_g.cu)
+bool launch_interp_line_g(const ConvArgs &a, int mode, cudaStream_t s);
 // FP32-mixed f-only interpolation on a BIN_GROUP binning (interp_group.cu)
 bool launch_interp_group(const ConvArgs &a, cudaStream_t s);
 // one warp per node on tile binnings (interp_tile_f32.cu, interp_tile_f64.cu)

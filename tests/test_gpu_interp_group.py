@@ -223,3 +223,49 @@ def test_grouped_kernel_runs(gpu):
     p.trafo(x, spectrum(np.random.default_rng(1), p))
     assert p.conv_kernel() == "tile"
     p.close()
+
+
+@pytest.mark.parametrize("cflags", [1 | 2, 2], ids=["f_grad", "grad"])
+@pytest.mark.parametrize("case", ["kaiser_bessel_m6", "gaussian_m2", "bspline_m4", "sinc_power_m5", "bessel_i0_m3",
+                                  "interlaced", "pre_cub_psi", "c2r", "odd_grid", "clustered", "accumulated"])
+def test_line_gradient_vs_oracle_and_per_node(gpu, oracle, case, cflags):
+    # the FP32-mixed interpolation with the gradient along lines (k_interp_line_g)
+    rng = np.random.default_rng(40)
+    N, n, m, flags, c2r, acc = (16, 16, 16), None, 6, 0, False, False
+    M = 3000
+    x = rng.uniform(-0.5, 0.5, (M, 3))
+    if "_m" in case:
+        win, mm = case.rsplit("_m", 1)
+        flags, m = WINDOWS[win], int(mm)
+    elif case == "interlaced":
+        flags = gpu.INTERLACED
+    elif case == "pre_cub_psi":
+        flags = gpu.PRE_CUB_PSI
+    elif case == "c2r":
+        c2r = True
+    elif case == "odd_grid":
+        N, m = (12, 18, 14), 5
+    elif case == "clustered":
+        x = np.concatenate([x[:500], 0.1 + 0.001 * rng.standard_normal((5000, 3))])
+    elif case == "accumulated":
+        acc = True
+    M = x.shape[0]
+    cf = cflags | (gpu.COMPUTE_ACCUMULATED if acc else 0)
+    dt = np.float64 if c2r else np.complex128
+    f0 = rng.standard_normal(M).astype(dt) if acc else None
+    g0 = rng.standard_normal((M, 3)).astype(dt) if acc else None
+    outs = []
+    for method in (0, 2):
+        p = gpu.Plan(N, n, m=m, flags=flags, c2r=c2r, precision="fp32")
+        p.set_conv_method(method)
+        fh = spectrum(np.random.default_rng(4), p)
+        kw = {} if not acc else {"f": None if f0 is None or not cflags & 1 else f0.copy(), "grad": g0.copy()}
+        outs.append(p.trafo(x, fh, cf, **kw))
+        assert p.conv_kernel() == ("line" if method == 0 else "tile")
+        p.close()
+    o = oracle.OraclePlan(N, n, m=m, flags=flags, c2r=c2r)
+    kw = {} if not acc else {"f": None if f0 is None or not cflags & 1 else f0.copy(), "grad": g0.copy()}
+    want = o.trafo(x, fh, cf, **kw)
+    for k in ((0, 1) if cflags & 1 else (1,)):
+        assert rel(outs[0][k], want[k]) < 1e-6, (case, k)
+        assert rel(outs[0][k], outs[1][k]) < 1e-6, (case, k)

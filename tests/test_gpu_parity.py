@@ -440,6 +440,6 @@ def test_x_max_below_half(gpu, oracle, prec, tol):
     p = gpu.Plan(N, n, m=m, x_max=xmax, precision=prec)
     assert p.lower_border == tuple(-xmax) and p.upper_border == tuple(xmax)
     o = oracle.OraclePlan(N, n, m=m)
-    for a, b in zip(p.trafo(x, fh, 1 | 2), o.trafo(x, fh, 1 | 2)):
+    for a, b in zip(p.trafo(x, fh, 1 | 2)[:2], o.trafo(x, fh, 1 | 2)[:2]):
         assert rel(a, b) < tol
     assert rel(p.adj(x, f), o.adj(x, f)) < tol
