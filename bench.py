@@ -487,9 +487,19 @@ def run_batched(P, torch, dev, steps=5):
             "eager_value": nodes / (ms_eager * 1e-3) / 1e6, "eager_ms": ms_eager,
             "plans": 65, "rhs_sharing_nodes": 8, "node_transforms_per_replay": nodes,
             "per_node_kernels_chosen": sum(1 for c in choice.values() if c[0] == 1),
+            "tunings_chosen": _count_tunings(choice),
             "max_rel_err_fp32_vs_fp64_trafo": max(errs),
             "workload": "64 plans N_t in {16..128}, M log-uniform [1e3, 2^21], KB m 4..6, trafo+adj each; "
                         "8 RHS on one node set M=2^20 at N=64^3; one CUDA graph"}
+
+
+def _count_tunings(choice):
+    """{"interp method/spread method/line sub-problem nodes": plans} over a batch's choices."""
+    out = {}
+    for c in choice.values():
+        key = "/".join(str(v) for v in c[2])
+        out[key] = out.get(key, 0) + 1
+    return out
 
 
 def run_particles(P, torch, dev, steps=3):
@@ -516,14 +526,21 @@ def run_particles(P, torch, dev, steps=3):
     for win, wflag in (("gaussian", P.WINDOW_GAUSSIAN), ("bspline", P.WINDOW_BSPLINE)):
         for grad, gflag in (("analytic", 0), ("ik", P.DIFF_IK)):
             p = P.Plan(N, m=m, flags=wflag | gflag, c2r=True, precision="fp32")
-            charges_c2r(p, xd, qd)
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(s)
-            for _ in range(steps):
-                fh, phi, gphi = charges_c2r(p, xd, qd)
-            b.record(s)
-            b.synchronize()
-            ms = a.elapsed_time(b) / steps
+
+            def timed():
+                charges_c2r(p, xd, qd)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(s)
+                for _ in range(steps):
+                    res = charges_c2r(p, xd, qd)
+                b.record(s)
+                b.synchronize()
+                return a.elapsed_time(b) / steps, res
+
+            ms_default, _ = timed()
+            fh0 = charges_c2r(p, xd, qd)[0]
+            tuning = p.autotune_device(xd, fh0, P.COMPUTE_F | P.COMPUTE_GRAD_F, P.COMPUTE_F)
+            ms, (fh, phi, gphi) = timed()
             ref = P.Plan(N, m=m, flags=wflag | gflag, c2r=True, precision="fp64")
             fh64 = ref.adj_device(xd, qd)
             sub = 4096
@@ -534,6 +551,7 @@ def run_particles(P, torch, dev, steps=3):
             torch.cuda.synchronize()
             rel = lambda u, v: (torch.linalg.vector_norm(u - v) / torch.linalg.vector_norm(v)).item()  # noqa: E731
             out[f"{win}_{grad}"] = {"value": M / (ms * 1e-3) / 1e6, "unit": "Mpts/s", "ms_per_step": ms,
+                                    "tuning": list(tuning), "ms_per_step_default_tuning": ms_default,
                                     "err_f_hat_vs_fp64": rel(fh, fh64),
                                     "err_phi_vs_fp64_ndft_4096": rel(phi[:sub], phid),
                                     "err_grad_vs_fp64_ndft_4096": rel(gphi[:sub], gphid),
@@ -542,7 +560,8 @@ def run_particles(P, torch, dev, steps=3):
             p.close()
             ref.close()
     out["workload"] = ("c2r, N=64^3, n=128^3, M=2^21 (20% in 64 clusters, sigma 0.01), charges +-1, m=5; "
-                       "step = adj + trafo(F|GRAD_F), FP32-mixed")
+                       "step = adj + trafo(F|GRAD_F), FP32-mixed; kernels chosen by pnfft_gb300_autotune "
+                       "(tuning = interp method, spread method, nodes per line sub-problem)")
     return out
 
 
@@ -552,8 +571,9 @@ def run_charge_dipole(P, steps=3):
     n = 128^3, Kaiser-Bessel m = 5, 2^20 charges and 2^18 dipoles uniform in
     [-0.5, 0.5)^3, host node arrays.  One pnfft_gb300_charge_dipole call
     (each node set copied and binned once, f_hat on the GPU throughout)
-    against the same four calls through pnfft_adj / pnfft_trafo.  Throughput
-    in particles per second; error of the energies against the FP64 call."""
+    against the same four calls through pnfft_adj / pnfft_trafo followed by
+    the energies and forces on the host (numpy).  Throughput in particles per
+    second; error of the energies against the FP64 call."""
     import ctypes
     from pnfft_gb300.particles import HostNodes, charge_dipole_host
     L = P.load()
@@ -595,7 +615,15 @@ def run_charge_dipole(P, steps=3):
                 fh += buf
                 L.pnfft_trafo(p._p, ch.handle, P.COMPUTE_F | P.COMPUTE_GRAD_F)
                 L.pnfft_trafo(p._p, di.handle, P.COMPUTE_GRAD_F | P.COMPUTE_HESSIAN_F)
+                # the energies and forces of the reference's test, on the host
+                e_c, f_c = q * ch.f, ch.grad_f * q[:, None]
+                e_d = (di.grad_f * mu).sum(1)
+                h = di.hessian_f
+                f_d = np.stack([h[:, 0] * mu[:, 0] + h[:, 1] * mu[:, 1] + h[:, 2] * mu[:, 2],
+                                h[:, 1] * mu[:, 0] + h[:, 3] * mu[:, 1] + h[:, 4] * mu[:, 2],
+                                h[:, 2] * mu[:, 0] + h[:, 4] * mu[:, 1] + h[:, 5] * mu[:, 2]], 1)
                 sep.append(time.perf_counter() - t0)
+            del e_c, f_c, e_d, f_d
             sep = sep[1:]
             t_fused = statistics.median(fused)
             t_sep = statistics.median(sep)

@@ -58,8 +58,8 @@ int pnfft_gb300_set_stream(pnfft_plan ths, void *cuda_stream);
  *      the same lines, other B one warp per node over a tile (cutoff and
  *      grid permitting);
  *  1 = one thread per node (small node counts on large grids);
- *  2 = B one warp per node over a tile also for the FP32-mixed f, and the
- *      FP32-mixed B^T of f with the register window that moves by copies;
+ *  2 = the FP32-mixed B one warp per node over 8x8x8 tiles (any output), and
+ *      the FP32-mixed B^T of f with the register window that moves by copies;
  *  3 = the FP32-mixed B of f in groups of nodes with overlapping stencils
  *      per warp (the same bits as 2). */
 int pnfft_gb300_set_conv_method(pnfft_plan ths, int method);
@@ -69,6 +69,23 @@ int pnfft_gb300_get_conv_method(const pnfft_plan ths);
  * per warp (FP32-mixed B), 2 one warp per node over a tile, 3 lines of tiles,
  * 4 one thread per node.  Set when the launch is issued. */
 int pnfft_gb300_get_conv_kernel(const pnfft_plan ths, int adjoint);
+
+/* Per-plan autotuning (no counterpart in the reference).  Times, on the
+ * given nodes and with the plan's current arrays (host or device), the
+ * kernel families of the interpolation (pnfft_trafo with trafo_flags) and of
+ * the spreading (pnfft_adj with adj_flags; 0 skips a direction) and the
+ * number of nodes per CTA of line binnings (256, 512, 2048), each binning
+ * included in its call's time, and keeps the fastest for this plan.  The
+ * transforms run as usual (the arrays receive their outputs); a node set
+ * whose distribution differs much from later ones may tune differently.
+ * pnfft_gb300_get_tuning returns (interpolation method, spreading method,
+ * nodes per line sub-problem).  Returns 0 on success. */
+int pnfft_gb300_autotune(pnfft_plan ths, pnfft_nodes nodes, unsigned trafo_flags, unsigned adj_flags, int reps);
+int pnfft_gb300_get_tuning(const pnfft_plan ths, int *tuning3);
+/* Sets the three values of pnfft_gb300_get_tuning (methods 0..3 as in
+ * pnfft_gb300_set_conv_method; nodes per line sub-problem a multiple of 32
+ * in [32, 4096]), e.g. a tuning saved from an earlier run. */
+int pnfft_gb300_set_tuning(pnfft_plan ths, const int *tuning3);
 
 /* Zero-copy mode.  When device arrays are attached, pnfft_trafo/pnfft_adj read
  * and write them directly and return without synchronizing the stream; the

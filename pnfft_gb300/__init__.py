@@ -239,9 +239,44 @@ class Plan:
         L.pnfft_gb300_set_device_f_hat(self._p, None)
 
     def set_conv_method(self, method):
-        """0: tiled interpolation / line-wise spreading (default); 1: one thread per node;
-        2: as 0 without node groups in the FP32-mixed interpolation."""
+        """Both directions: 0 line kernels (default); 1 one thread per node; 2 the
+        FP32-mixed B one warp per node over 8x8x8 tiles and B^T with the window
+        that moves by copies; 3 as 2 with groups of nodes for f alone."""
         _check(load().pnfft_gb300_set_conv_method(self._p, int(method)), "set_conv_method")
+
+    def tuning(self):
+        """(interpolation method, spreading method, nodes per line sub-problem)."""
+        t = (ctypes.c_int * 3)()
+        _check(load().pnfft_gb300_get_tuning(self._p, t), "get_tuning")
+        return tuple(t)
+
+    def set_tuning(self, tuning):
+        """Restore a tuning() triple."""
+        t = (ctypes.c_int * 3)(*[int(v) for v in tuning])
+        _check(load().pnfft_gb300_set_tuning(self._p, t), "set_tuning")
+
+    def autotune_device(self, x, f_hat, trafo_flags=COMPUTE_F, adj_flags=COMPUTE_F, reps=2):
+        """pnfft_gb300_autotune on CUDA tensors: times the kernel families and the
+        line sub-problem size on the nodes x for a trafo with trafo_flags and an
+        adjoint with adj_flags (0: not used) and keeps the fastest; returns
+        tuning().  The transforms run on scratch node arrays and a copy of
+        f_hat; the arguments are left unchanged."""
+        import torch
+        dt = torch.float64 if self.c2r else torch.complex128
+        M = x.shape[0]
+        grad = (trafo_flags | adj_flags) & COMPUTE_GRAD_F
+        fo = torch.zeros(M, dtype=dt, device=x.device)
+        go = torch.zeros(M, 3, dtype=dt, device=x.device) if grad else None
+        ho = torch.zeros(M, 6, dtype=dt, device=x.device) if trafo_flags & COMPUTE_HESSIAN_F else None
+        fh = f_hat.clone()
+        s = _stream_handle(torch.cuda.current_stream(x.device))
+        L = load()
+        nd = self._bind_device(x, fo, go, ho, fh, s)
+        L.pnfft_gb300_clear_error()
+        rc = L.pnfft_gb300_autotune(self._p, nd, ctypes.c_uint(trafo_flags), ctypes.c_uint(adj_flags), int(reps))
+        self.synchronize()
+        _check(rc, "pnfft_gb300_autotune")
+        return self.tuning()
 
     CONV_KERNELS = {0: "none", 1: "group", 2: "tile", 3: "line", 4: "generic"}
 

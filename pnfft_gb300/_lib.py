@@ -174,6 +174,9 @@ SIGNATURES = {
     "pnfft_gb300_last_stage_ms": (_I, [_P, _I, _DP]),
     "pnfft_gb300_measure_fp32_fma": (_I, [_I, _DP]),
     "pnfft_gb300_charge_dipole": (_I, [_P, _P, _P, _U, _P, _P]),
+    "pnfft_gb300_autotune": (_I, [_P, _P, _U, _U, _I]),
+    "pnfft_gb300_get_tuning": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "pnfft_gb300_set_tuning": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
 }
 
 _lib = None

@@ -8,9 +8,9 @@ A batch is a list of transforms on device-resident torch tensors:
 ``Batch`` runs every item once, eagerly, so that the first call allocates
 each plan's grid, FFT plan, window tables and node binning. The node sets
 are declared fixed, so the binning is computed once and reused. It can then
-pick each plan's convolution kernels by timing them (``autotune``: the tiled
-interpolation / line-wise spreading kernels against the one-thread-per-node
-kernels, which win for small M on large grids). Finally it captures all items
+pick each plan's convolution kernels by timing them (``autotune``: the line
+kernels, the FP32-mixed tile kernels and the one-thread-per-node kernels,
+which win for small M on large grids). Finally it captures all items
 on one stream into a single CUDA graph. ``run()`` replays the whole batch with
 one graph launch, so the per-call host work of the C library (argument
 checks, stream and pointer setup, about 50 launches per item) is paid once
@@ -79,16 +79,26 @@ class Batch:
         return a.elapsed_time(b) / reps
 
     def autotune(self, reps=3):
-        """Per plan: time the tiled / line kernels (0) against the per-node
-        kernels (1) on the plan's own items and keep the faster."""
+        """Per plan, on the plan's own items: pnfft_gb300_autotune on the nodes
+        of the plan's first item (with the flags of its first trafo and first
+        adjoint) picks the kernel family of each direction and the
+        line sub-problem size ("auto"); that tuning is then timed against the
+        one-thread-per-node kernels (method 1) on all of the plan's items and
+        the faster kept.  choice[id(plan)] = (winner, {candidate: ms per
+        replay of the plan's items}, tuning())."""
         for p in self._plans():
-            t = {}
-            for method in (0, 1):
-                p.set_conv_method(method)
-                t[method] = self._time_plan(p, reps)
+            mine = [it for it in self.items if it[1] is p]
+            tr = next((it for it in mine if it[0] == "trafo"), None)
+            ad = next((it for it in mine if it[0] == "adj"), None)
+            x, f_hat = mine[0][2], mine[0][3]
+            auto = p.autotune_device(x, f_hat, tr[7] if tr else 0, ad[7] if ad else 0, reps=1)
+            t = {"auto": self._time_plan(p, reps)}
+            p.set_conv_method(1)
+            t[1] = self._time_plan(p, reps)
             best = min(t, key=t.get)
-            p.set_conv_method(best)
-            self.choice[id(p)] = (best, t)
+            if best == "auto":
+                p.set_tuning(auto)
+            self.choice[id(p)] = (best, t, p.tuning())
         self.graph = None
         return self.choice
 

@@ -325,6 +325,7 @@ static pnfft_plan init_guru_internal(int d, const ptrdiff_t *N, const ptrdiff_t 
   if (pnfft_flags & PNFFT_PRE_GRAD_PSI) pnfft_flags |= PNFFT_PRE_PSI;
 
   pnfft_plan p = new pnfft_plan_s();
+  p->line_sub_max = 512;
   p->d = 3;
   p->m = m;
   p->cutoff = 2 * m + 1;
@@ -924,10 +925,41 @@ extern "C" int pnfft_gb300_set_conv_method(pnfft_plan ths, int method) {
               method);
     return -1;
   }
-  ths->conv_method = method;
+  ths->conv_method[0] = ths->conv_method[1] = method;
   return 0;
 }
-extern "C" int pnfft_gb300_get_conv_method(const pnfft_plan ths) { return ths ? ths->conv_method : -1; }
+extern "C" int pnfft_gb300_get_conv_method(const pnfft_plan ths) { return ths ? ths->conv_method[0] : -1; }
+extern "C" int pnfft_gb300_get_tuning(const pnfft_plan ths, int *tuning) {
+  if (!ths || !tuning) return -1;
+  tuning[0] = ths->conv_method[0];
+  tuning[1] = ths->conv_method[1];
+  tuning[2] = ths->line_sub_max;
+  return 0;
+}
+extern "C" int pnfft_gb300_set_tuning(pnfft_plan ths, const int *tuning) {
+  if (!ths || !tuning) return -1;
+  for (int d = 0; d < 2; d++)
+    if (tuning[d] < 0 || tuning[d] > 3) {
+      set_error("pnfft_gb300_set_tuning: unknown method %d", tuning[d]);
+      return -1;
+    }
+  if (tuning[2] < 32 || tuning[2] > 4096 || (tuning[2] & 31)) {
+    set_error("pnfft_gb300_set_tuning: nodes per line sub-problem %d not a multiple of 32 in [32, 4096]", tuning[2]);
+    return -1;
+  }
+  ths->conv_method[0] = tuning[0];
+  ths->conv_method[1] = tuning[1];
+  ths->line_sub_max = tuning[2];
+  return 0;
+}
+extern "C" int pnfft_gb300_autotune(pnfft_plan ths, pnfft_nodes nodes, unsigned trafo_flags, unsigned adj_flags,
+                                    int reps) {
+  if (!ths || !nodes) {
+    set_error("pnfft_gb300_autotune: plan and nodes are required");
+    return -1;
+  }
+  return engine_autotune(ths, nodes, trafo_flags, adj_flags, reps > 0 ? reps : 2);
+}
 extern "C" int pnfft_gb300_get_conv_kernel(const pnfft_plan ths, int adjoint) {
   return ths ? ths->last_conv[adjoint ? 1 : 0] : -1;
 }

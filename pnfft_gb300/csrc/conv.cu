@@ -303,11 +303,11 @@ void choose_tiles(int cut, bool fp32, bool spread, bool f_only, int method, cons
   // for every kernel where the cutoff allows: the line kernels of B^T and of
   // the FP32-mixed B of f, and the one-warp-per-node B over each 4x4x4 tile's
   // (3+cutoff)^3 region for the other interpolations -- one binning serves both
-  // directions.  Conv methods 2 and 3 of the FP32-mixed B of f take 8x8x8
-  // tiles (one warp per node, or groups of nodes per warp).
+  // directions.  Conv methods 2 and 3 of the FP32-mixed B take 8x8x8 tiles
+  // (one warp per node; groups of nodes per warp for f alone with method 3).
   *line_mode = BIN_TILE;
   const bool lines_fit = n[0] >= 4 && n[1] >= 4 && n[2] >= 4 && n[2] < 32768 && cut <= 15;
-  const bool tiles8 = !spread && fp32 && f_only && (method == 2 || method == 3);
+  const bool tiles8 = !spread && fp32 && (method == 2 || method == 3);
   if (lines_fit && !tiles8) {
     T[0] = T[1] = T[2] = 4;
     *line_mode = BIN_LINE;

@@ -330,9 +330,11 @@ static BinSlot *ensure_binning(pnfft_plan p, pnfft_nodes nd, int spread, int il,
   const int64_t M = nd->local_M;
   int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
   int T[3], line_mode = 0;
-  choose_tiles(p->cutoff, fp32(p), spread != 0, f_only, p->conv_method, n, M, T, &line_mode);
+  choose_tiles(p->cutoff, fp32(p), spread != 0, f_only, p->conv_method[spread ? 1 : 0], n, M, T, &line_mode);
   BinSlot &sl = node_dev(nd)->bins[line_mode == BIN_LINE ? 0 : 1][il];
-  bool same = T[0] == sl.T[0] && T[1] == sl.T[1] && T[2] == sl.T[2] && line_mode == sl.line_mode;
+  const int sub_max = line_mode == BIN_LINE ? p->line_sub_max : 1024;
+  bool same = T[0] == sl.T[0] && T[1] == sl.T[1] && T[2] == sl.T[2] && line_mode == sl.line_mode &&
+              sl.b.sub_max == sub_max;
   for (int t = 0; t < 3; t++) same = same && sl.b.ntile[t] == (n[t] + T[t] - 1) / T[t];
   if (same && sl.cap >= M && sl.b.key && sl.prec == p->precision) return &sl;
   int64_t cap = std::max<int64_t>(M, std::max<int64_t>(sl.cap, 1));
@@ -346,7 +348,10 @@ static BinSlot *ensure_binning(pnfft_plan p, pnfft_nodes nd, int spread, int il,
   b.ntiles = b.ntile[0] * b.ntile[1] * b.ntile[2];
   b.line_mode = line_mode;
   b.nkeys = line_mode == BIN_GROUP ? b.ntiles * kBlocksPerTile : b.ntiles;
-  b.sub_max = line_mode == BIN_LINE ? 2048 : 1024;
+  // line binnings: at most line_sub_max nodes of a line per CTA (512 unless
+  // tuned): dense clusters put thousands of nodes on a few lines, which would
+  // otherwise run long after the others
+  b.sub_max = sub_max;
   const int units = line_mode == BIN_LINE ? b.ntile[0] * b.ntile[1] : b.ntiles;
   b.max_subs = (int)(units + cap / b.sub_max + 1);
   b.max_tsubs = line_mode == BIN_LINE ? (int)(b.ntiles + cap / b.sub_max + 1) : 0;
@@ -740,8 +745,8 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       ConvArgs ca;
       memset(&ca, 0, sizeof(ca));
       ca.w = window_args(p);
-      ca.generic = p->conv_method == 1;
-      ca.method = p->conv_method;
+      ca.generic = p->conv_method[0] == 1;
+      ca.method = p->conv_method[0];
       ca.real_only = p->c2r || (p->pnfft_flags & PNFFT_PRE_QUAD_PSI) ? 1 : 0;
       ca.real_io = p->c2r;
       ca.M = M;
@@ -898,8 +903,8 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       ConvArgs ca;
       memset(&ca, 0, sizeof(ca));
       ca.w = window_args(p);
-      ca.generic = p->conv_method == 1;
-      ca.method = p->conv_method;
+      ca.generic = p->conv_method[1] == 1;
+      ca.method = p->conv_method[1];
       ca.real_only = 0;
       ca.real_io = p->c2r;
       ca.M = M;
@@ -971,6 +976,84 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
     PG_CUDA(cudaStreamSynchronize(s));
     engine_flush_timers(p);
   }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// autotuning: the kernel family of each direction and the sub-problem size of
+// line binnings, timed on the caller's nodes
+//
+// Candidates: interpolation with the line kernels (method 0) or one warp per
+// node over 8x8x8 tiles (method 2, FP32-mixed); spreading with the rotating
+// register window (0) or the window that moves by copies (2); line
+// sub-problems of 256, 512 or 2048 nodes.  Each candidate runs `reps` timed
+// calls (after one untimed call) with the node set treated as changing (it is
+// binned in every call, as pnfft_trafo / pnfft_adj do), and the time of a call
+// is its binning plus its convolution (stage timers).  The plan keeps, per
+// direction, the fastest method, and the sub-problem size with the smallest
+// sum over both directions.  The transforms write their outputs as usual.
+// ---------------------------------------------------------------------------
+static int time_call(pnfft_plan p, pnfft_nodes nd, bool adjoint, unsigned flags, int reps, double *ms) {
+  double best = 1e300;
+  for (int r = 0; r <= reps; r++) {
+    nd->version++;  // re-bin as for changing coordinates
+    if ((adjoint ? engine_adj(p, nd, flags) : engine_trafo(p, nd, flags)) || engine_sync(p)) return -1;
+    const double t = p->last_ms[adjoint ? 1 : 0][PNFFT_TIMER_SORT_NODES] + p->last_ms[adjoint ? 1 : 0][PNFFT_TIMER_MATRIX_B];
+    if (r > 0) best = std::min(best, t);
+  }
+  *ms = best;
+  return 0;
+}
+
+int engine_autotune(pnfft_plan p, pnfft_nodes nd, unsigned trafo_flags, unsigned adj_flags, int reps) {
+  const int keep[2] = {p->conv_method[0], p->conv_method[1]}, keep_sub = p->line_sub_max;
+  const int subs[3] = {256, 512, 2048};
+  const int methods[2] = {0, 2};
+  const int nm = fp32(p) ? 2 : 1;  // FP64 plans have one family per direction
+  double best_total = 1e300;
+  int best[3] = {keep[0], keep[1], keep_sub};
+  const int fixed = nd->fixed;
+  nd->fixed = 0;
+  for (int si = 0; si < 3; si++) {
+    p->line_sub_max = subs[si];
+    double bt[2] = {1e300, 1e300};
+    int bm[2] = {0, 0};
+    for (int dir = 0; dir < 2; dir++) {
+      const unsigned flags = dir ? adj_flags : trafo_flags;
+      if (!flags) {
+        bt[dir] = 0.0;
+        bm[dir] = keep[dir];
+        continue;
+      }
+      for (int mi = 0; mi < nm; mi++) {
+        p->conv_method[dir] = methods[mi];
+        double ms = 0.0;
+        if (time_call(p, nd, dir == 1, flags, reps, &ms)) {
+          p->conv_method[0] = keep[0];
+          p->conv_method[1] = keep[1];
+          p->line_sub_max = keep_sub;
+          nd->fixed = fixed;
+          return -1;
+        }
+        if (ms < bt[dir]) {
+          bt[dir] = ms;
+          bm[dir] = methods[mi];
+        }
+      }
+      p->conv_method[dir] = bm[dir];
+    }
+    if (bt[0] + bt[1] < best_total) {
+      best_total = bt[0] + bt[1];
+      best[0] = bm[0];
+      best[1] = bm[1];
+      best[2] = subs[si];
+    }
+  }
+  p->conv_method[0] = best[0];
+  p->conv_method[1] = best[1];
+  p->line_sub_max = best[2];
+  nd->fixed = fixed;
+  nd->version++;
   return 0;
 }
 

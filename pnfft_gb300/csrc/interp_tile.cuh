@@ -247,13 +247,19 @@ static bool interp_tile_by_cut(const ConvArgs &a, cudaStream_t s) {
   }
 }
 
-// 4x4x4 tiles of a line binning in every mode; 8x8x8 tiles only for the
-// FP32-mixed f (conv methods 2 and 3)
+// 4x4x4 tiles of a line binning in every mode; 8x8x8 tiles for the
+// FP32-mixed plans (conv methods 2 and 3)
 template <typename T>
 static bool interp_tile_t(const ConvArgs &a, int mode, cudaStream_t s) {
   if (a.bin.T[0] == 8) {
-    if (sizeof(T) == 4 && mode == 1) return interp_tile_by_cut<T, 1, 8>(a, s);
-    return false;
+    if (sizeof(T) != 4) return false;
+    switch (mode) {
+      case 1: return interp_tile_by_cut<T, 1, 8>(a, s);
+      case 2: return interp_tile_by_cut<T, 2, 8>(a, s);
+      case 3: return interp_tile_by_cut<T, 3, 8>(a, s);
+      case 4: return interp_tile_by_cut<T, 4, 8>(a, s);
+      default: return false;
+    }
   }
   if (a.bin.T[0] != 4) return false;
   switch (mode) {

@@ -39,8 +39,9 @@ struct pnfft_plan_s {
   double timer_adj[PNFFT_TIMER_LENGTH];
   double last_ms[2][PNFFT_TIMER_LENGTH];
   int precision;      // PNFFT_GB300_FP64 / PNFFT_GB300_FP32_MIXED
-  int conv_method;    // 0: tiled/line kernels where usable, 1: one thread per node,
-                      // 2: tiled without node groups in the FP32-mixed interpolation
+  int conv_method[2];  // [interpolation, spreading]: pnfft_gb300_set_conv_method (both),
+                       // or per direction by pnfft_gb300_autotune
+  int line_sub_max;    // nodes of a line per CTA (sub-problem) in line binnings
   int last_conv[2];   // pg::ConvKernel of the last B / B^T launch
   void *d_f_hat_user; // zero-copy f_hat
   void *user_stream;
@@ -71,6 +72,7 @@ const char *last_error();
 // engine.cu
 int engine_trafo(pnfft_plan ths, pnfft_nodes nodes, unsigned cflags);
 int engine_adj(pnfft_plan ths, pnfft_nodes nodes, unsigned cflags);
+int engine_autotune(pnfft_plan ths, pnfft_nodes nodes, unsigned trafo_flags, unsigned adj_flags, int reps);
 int engine_charge_dipole(pnfft_plan ths, pnfft_nodes charges, pnfft_nodes dipoles, unsigned cflags, void *energy,
                          void *force);
 int engine_set_stream(pnfft_plan ths, void *stream);

@@ -69,6 +69,33 @@ class HostNodes:
             pass
 
 
+class _Pinned(np.ndarray):
+    """A numpy array over page-locked memory from pnfft_alloc_complex, freed with it."""
+
+    def __array_finalize__(self, obj):
+        self._owner = getattr(obj, "_owner", None)
+
+
+class _Block:
+    def __init__(self, n):
+        self.ptr = load().pnfft_alloc_complex(max(int(n), 1))
+
+    def __del__(self):
+        try:
+            load().pnfft_free(self.ptr)
+        except Exception:
+            pass
+
+
+def _pinned_complex(n):
+    blk = _Block(n)
+    raw = np.ctypeslib.as_array(ctypes.cast(blk.ptr, ctypes.POINTER(ctypes.c_double)), (2 * max(int(n), 1),))
+    arr = raw[:2 * int(n)].view(np.complex128).view(_Pinned)
+    arr._owner = blk
+    arr[...] = 0
+    return arr
+
+
 def charge_dipole_host(plan, charges, dipoles, compute_flags=0):
     """The sequence of charge_dipole on HostNodes through pnfft_gb300_charge_dipole.
 
@@ -78,8 +105,7 @@ def charge_dipole_host(plan, charges, dipoles, compute_flags=0):
     """
     L = load()
     M = charges.M + dipoles.M
-    energy = np.zeros(M, np.complex128)
-    force = np.zeros((M, 3), np.complex128)
+    energy, force = _pinned_complex(M), _pinned_complex(3 * M).reshape(M, 3)
     S = int(np.prod(plan.local_N))
     f_hat = np.zeros(S, np.complex128)
     L.pnfft_set_f_hat(f_hat.ctypes.data, plan._p)

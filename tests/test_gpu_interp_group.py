@@ -190,9 +190,9 @@ def test_line_variants_vs_oracle(gpu, oracle, case):
 
 def test_grouped_kernel_runs(gpu):
     # the kernel family each call launched (pnfft_gb300_get_conv_kernel): lines
-    # for f by default and for B^T; groups with method 3 (not with too few
-    # nodes per corner block); one warp per node for method 2, the gradient
-    # and the Hessian
+    # for f and f + gradient by default and for B^T; groups with method 3 (not
+    # with too few nodes per corner block); one warp per node for method 2 and
+    # for the Hessian
     N = (16, 16, 16)
     rng = np.random.default_rng(5)
     x = rng.uniform(-0.5, 0.5, (3000, 3))
@@ -214,7 +214,8 @@ def test_grouped_kernel_runs(gpu):
     assert kernel(3, gpu.COMPUTE_F) == "group"
     assert kernel(2, gpu.COMPUTE_F) == "tile"
     assert kernel(1, gpu.COMPUTE_F) == "generic"
-    assert kernel(0, gpu.COMPUTE_F | gpu.COMPUTE_GRAD_F) == "tile"
+    assert kernel(0, gpu.COMPUTE_F | gpu.COMPUTE_GRAD_F) == "line"
+    assert kernel(2, gpu.COMPUTE_F | gpu.COMPUTE_GRAD_F) == "tile"
     assert kernel(0, gpu.COMPUTE_HESSIAN_F) == "tile"
     assert kernel(3, gpu.COMPUTE_F, nodes=x[:500]) == "tile"  # 500 nodes on 2048 corner blocks
     assert kernel(0, gpu.COMPUTE_F, adjoint=True) == "line"
