@@ -387,9 +387,9 @@ def run_gpu(args):
     L.pnfft_free_nodes(nodes, P.FREE_X | P.FREE_F)
     L.pnfft_finalize(plan, P.FREE_F_HAT)
 
-    # trafo: binning (keys, 3 scans, scatter, sub-problems) + D + B; adj: binning
-    # (keys, 3 scans, scatter, line sub-problems) + B^T + D^T (cuFFT not counted)
-    launches_per_step = 16
+    # trafo: binning (keys, 3 scans, scatter, tile sub-problems, line
+    # sub-problems) + D + B; adj: the same binning + B^T + D^T (cuFFT not counted)
+    launches_per_step = 18
     line = {"metric": METRIC, "value": value, "unit": "Mpts/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",

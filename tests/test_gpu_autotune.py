@@ -82,7 +82,7 @@ def test_autotune_host_arrays_and_set_tuning(gpu, oracle):
     # host arrays of the plan's nodes, alive through the C call
     xh = np.ascontiguousarray(x)
     fo = np.zeros(M, np.complex128)
-    fhh = np.ascontiguousarray(fh.ravel())
+    fhh = fh.ravel().copy()  # the adjoint of the autotuner writes its f_hat here
     nd = p._nodes_for(M)
     L.pnfft_set_x(xh.ctypes.data, nd)
     L.pnfft_set_f(fo.ctypes.data, nd)
