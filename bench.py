@@ -415,6 +415,7 @@ def run_gpu(args):
         line["batched"] = run_batched(P, torch, dev)
         line["particles"] = run_particles(P, torch, dev)
         line["charge_dipole"] = run_charge_dipole(P)
+        line["float_api"] = run_float_api(P, x, fh, f)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(inputs=(x, fh, f))[0].items()
                                 if k != "seconds_per_step"}
@@ -500,6 +501,63 @@ def _count_tunings(choice):
         key = "/".join(str(v) for v in c[2])
         out[key] = out.get(key, 0) + 1
     return out
+
+
+def run_float_api(P, x, fh, f, steps=3):
+    """The single-precision API pnfftf_* end to end on the bench workload
+    (N=128^3, n=256^3, M=2^22, Kaiser-Bessel m=6): float host arrays
+    (page-locked, PNFFT_MALLOC_*), one pnfftf_trafo (COMPUTE_F) + one
+    pnfftf_adj per step, each call copying float arrays to the GPU, widening
+    and rounding there.  Wall-clock time of the two calls; the float results
+    against the double API's FP32-mixed results on the same (float) inputs."""
+    import ctypes
+    L = P.load()
+    Pp, U = ctypes.c_void_p, ctypes.c_uint
+    for k, (r, a) in {"pnfftf_init_guru": (Pp, [ctypes.c_int, Pp, Pp, Pp, ctypes.c_int, U, U, ctypes.c_int]),
+                      "pnfftf_init_nodes": (Pp, [ctypes.c_ssize_t, U]), "pnfftf_get_x": (Pp, [Pp]),
+                      "pnfftf_get_f": (Pp, [Pp]), "pnfftf_get_f_hat": (Pp, [Pp]),
+                      "pnfftf_trafo": (None, [Pp, Pp, U]), "pnfftf_adj": (None, [Pp, Pp, U]),
+                      "pnfftf_finalize": (None, [Pp, U]), "pnfftf_free_nodes": (None, [Pp, U])}.items():
+        getattr(L, k).restype = r
+        getattr(L, k).argtypes = a
+    N, n, M, m = CFG["N"], CFG["n"], CFG["M"], CFG["m"]
+    Nc, nc = (ctypes.c_ssize_t * 3)(*N), (ctypes.c_ssize_t * 3)(*n)
+    p = L.pnfftf_init_guru(3, Nc, nc, (ctypes.c_float * 3)(0.5, 0.5, 0.5), m, P.MALLOC_F_HAT, P.PFFT_ESTIMATE,
+                           P.MPI_COMM_WORLD)
+    nd = L.pnfftf_init_nodes(M, P.MALLOC_X | P.MALLOC_F)
+    fv = lambda ptr, k: np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ctypes.c_float)), (k,))  # noqa: E731
+    hx, hf, hfh = fv(L.pnfftf_get_x(nd), 3 * M), fv(L.pnfftf_get_f(nd), 2 * M), fv(L.pnfftf_get_f_hat(p), 2 * fh.size)
+    x32, fh32, f32 = x.astype(np.float32), fh.astype(np.complex64), f.astype(np.complex64)
+    hx[:] = x32.ravel()
+    times = []
+    for it in range(steps + 1):
+        hfh[:] = fh32.view(np.float32)
+        t0 = time.perf_counter()
+        L.pnfftf_trafo(p, nd, P.COMPUTE_F)
+        t1 = time.perf_counter()
+        out_f = hf.copy().view(np.complex64)
+        hf[:] = f32.view(np.float32)
+        t2 = time.perf_counter()
+        L.pnfftf_adj(p, nd, P.COMPUTE_F)
+        t3 = time.perf_counter()
+        if it:
+            times.append((t1 - t0) + (t3 - t2))
+    out_fh = hfh.copy().view(np.complex64)
+    L.pnfftf_free_nodes(nd, P.FREE_X | P.FREE_F)
+    L.pnfftf_finalize(p, P.FREE_F_HAT)
+    # the double API, FP32-mixed, on the same float-rounded inputs
+    q = P.Plan(N, n, m=m, precision="fp32")
+    xd = x32.astype(np.float64)
+    ref_f = q.trafo(xd, fh32.astype(np.complex128))[0]
+    ref_fh = q.adj(xd, f32.astype(np.complex128))
+    q.close()
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+    ms = 1e3 * statistics.mean(times)
+    return {"value": M / (ms * 1e-3) / 1e6, "unit": "Mpts/s", "ms_per_step": ms,
+            "h2d_bytes_per_step": 2 * M * 12 + fh.size * 8 + M * 8, "d2h_bytes_per_step": M * 8 + fh.size * 8,
+            "rel_diff_f_vs_double_api": rel(out_f, ref_f), "rel_diff_f_hat_vs_double_api": rel(out_fh, ref_fh),
+            "workload": "pnfftf_trafo + pnfftf_adj, float host arrays (page-locked), N=128^3, n=256^3, M=2^22, "
+                        "KB m=6; conversions on the GPU"}
 
 
 def run_particles(P, torch, dev, steps=3):

@@ -19,7 +19,7 @@ INC = os.path.join(os.path.dirname(HERE), "include")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["conv.cu", "interp_line.cu", "interp_line_g.cu", "spread_line_f.cu", "interp_group.cu", "interp_tile_f32.cu", "interp_tile_f64.cu", "spread_line_f32.cu",
+CU_SOURCES = ["conv.cu", "float_io.cu", "interp_line.cu", "interp_line_g.cu", "spread_line_f.cu", "interp_group.cu", "interp_tile_f32.cu", "interp_tile_f64.cu", "spread_line_f32.cu",
               "spread_line_f64.cu", "generic.cu", "deconv.cu", "sort.cu", "ndft.cu", "engine.cu", "peak.cu"]
 CPP_SOURCES = ["api.cpp", "api_float.cpp"]
 

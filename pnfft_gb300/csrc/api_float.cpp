@@ -1,12 +1,11 @@
 // api_float.cpp -- the single-precision API pnfftf_* (the float expansion of
 // PNFFT_DEFINE_API, api/pnfft.h:287) as a layer over the double library.
 //
-// A float plan wraps a double plan that owns a page-locked double f_hat, and
-// runs in the FP32-mixed precision of the GPU path (FP64 when the window would
-// overflow FP32).  Float nodes wrap double nodes whose x / f / grad_f /
-// hessian_f point at page-locked double staging arrays allocated on first use.
-// pnfftf_trafo / pnfftf_adj convert the caller's float arrays into the
-// staging arrays, run the double call, and round the outputs back to float.
+// A float plan wraps a double plan and runs in the FP32-mixed precision of the
+// GPU path (FP64 when the window would overflow FP32); float nodes wrap double
+// nodes.  pnfftf_trafo / pnfftf_adj (float_io.cu) copy the caller's float
+// arrays to the GPU, widen them there, run the double plan on those device
+// arrays and round the outputs to float on the GPU before copying them back.
 // Ownership and flag semantics are those of the double API (api-basic.c:402-442).
 #include <math.h>
 #include <stdio.h>
@@ -14,34 +13,12 @@
 #include <string.h>
 
 #include "../../include/pnfft.h"
-
-struct pnfftf_plan_s {
-  pnfft_plan p;     // double plan (PNFFT_MALLOC_F_HAT: its f_hat is the staging array)
-  float *f_hat;     // caller's or own interleaved complex float array
-  int own_f_hat;
-  ptrdiff_t nfh;    // complex entries of f_hat (local_N total)
-  int c2r;
-};
-
-struct pnfftf_nodes_s {
-  pnfft_nodes nd;   // double nodes pointing at the staging arrays below
-  ptrdiff_t M;
-  float *x, *f, *grad, *hess;  // caller's or own float arrays (complex: interleaved)
-  double *sx, *sf, *sgrad, *shess;
-};
+#include "api_float.h"
 
 namespace {
 
-double *staging(double **slot, size_t n) {
-  if (!*slot) *slot = (double *)pnfft_malloc(sizeof(double) * (n > 0 ? n : 1));
-  return *slot;
-}
-
 void to_double(double *d, const float *s, size_t n) {
   for (size_t i = 0; i < n; i++) d[i] = (double)s[i];
-}
-void to_float(float *d, const double *s, size_t n) {
-  for (size_t i = 0; i < n; i++) d[i] = (float)s[i];
 }
 
 pnfftf_plan wrap(pnfft_plan p, int c2r, unsigned pnfft_flags, const ptrdiff_t *local_N) {
@@ -180,7 +157,8 @@ pnfft_plan pnfftf_gb300_double_plan(pnfftf_plan ths) { return ths ? ths->p : nul
 void pnfftf_finalize(pnfftf_plan ths, unsigned pnfft_finalize_flags) {
   if (!ths) return;
   if ((pnfft_finalize_flags & PNFFT_FREE_F_HAT) && ths->f_hat) pnfft_free(ths->f_hat);
-  pnfft_finalize(ths->p, PNFFT_FREE_F_HAT);  // the double staging f_hat
+  pnfft_finalize(ths->p, PNFFT_FREE_F_HAT);  // synchronizes the plan's stream
+  pg::float_dev_free(ths->dev);
   free(ths);
 }
 
@@ -204,22 +182,14 @@ void pnfftf_free_nodes(pnfftf_nodes nodes, unsigned pnfft_finalize_flags) {
   if ((pnfft_finalize_flags & PNFFT_FREE_GRAD_F) && nodes->grad) pnfft_free(nodes->grad);
   if ((pnfft_finalize_flags & PNFFT_FREE_HESSIAN_F) && nodes->hess) pnfft_free(nodes->hess);
   pnfft_free_nodes(nodes->nd, 0);
-  double *st[4] = {nodes->sx, nodes->sf, nodes->sgrad, nodes->shess};
-  for (double *s : st)
-    if (s) pnfft_free(s);
+  pg::float_dev_free(nodes->dev);
   free(nodes);
 }
 
-static void stage_x(pnfftf_nodes nodes) {
-  const size_t n = 3 * (size_t)nodes->M;
-  double *sx = staging(&nodes->sx, n);
-  if (nodes->x) to_double(sx, nodes->x, n);
-  pnfft_set_x(sx, nodes->nd);
-}
-
+// the window values are evaluated on the fly (pnfft_precompute_psi); what
+// the call keeps is the promise that the coordinates stay fixed
 void pnfftf_precompute_psi(pnfftf_plan ths, pnfftf_nodes nodes, unsigned precompute_flags) {
   if (!ths || !nodes) return;
-  stage_x(nodes);
   pnfft_precompute_psi(ths->p, nodes->nd, precompute_flags);
 }
 
@@ -264,58 +234,14 @@ void pnfftf_get_b(const pnfftf_plan ths, float *b0, float *b1, float *b2) {
 }
 
 // --- transforms ------------------------------------------------------------------
-// Each node array in use is staged as doubles (page-locked); outputs that are
-// accumulated (COMPUTE_ACCUMULATED) are staged before the call as well.
 void pnfftf_trafo(pnfftf_plan ths, pnfftf_nodes nodes, unsigned compute_flags) {
   if (!ths || !nodes) return;  // api-basic.c:205-206
-  const size_t M = (size_t)(nodes->M > 0 ? nodes->M : 0), tu = tuple(ths);
-  const bool acc = (compute_flags & PNFFT_COMPUTE_ACCUMULATED) != 0;
-  double *fh = (double *)pnfft_get_f_hat(ths->p);
-  if (ths->f_hat && fh) to_double(fh, ths->f_hat, 2 * (size_t)ths->nfh);
-  stage_x(nodes);
-  struct Out {
-    unsigned flag;
-    float *user;
-    double **slot;
-    size_t comps;
-  } outs[3] = {{PNFFT_COMPUTE_F, nodes->f, &nodes->sf, 1},
-               {PNFFT_COMPUTE_GRAD_F, nodes->grad, &nodes->sgrad, 3},
-               {PNFFT_COMPUTE_HESSIAN_F, nodes->hess, &nodes->shess, 6}};
-  double *ptr[3] = {nullptr, nullptr, nullptr};
-  for (int k = 0; k < 3; k++) {
-    if (!(compute_flags & outs[k].flag) || !outs[k].user) continue;
-    const size_t n = outs[k].comps * M * tu;
-    ptr[k] = staging(outs[k].slot, outs[k].comps * M * 2);
-    if (acc) to_double(ptr[k], outs[k].user, n);
-  }
-  pnfft_set_f((pnfft_complex *)ptr[0], nodes->nd);
-  pnfft_set_grad_f((pnfft_complex *)ptr[1], nodes->nd);
-  pnfft_set_hessian_f((pnfft_complex *)ptr[2], nodes->nd);
-  pnfft_trafo(ths->p, nodes->nd, compute_flags);
-  for (int k = 0; k < 3; k++)
-    if (ptr[k]) to_float(outs[k].user, ptr[k], outs[k].comps * M * tu);
+  if (pnfftf_gb300_trafo_dev(ths, nodes, compute_flags)) fprintf(stderr, "pnfftf_trafo: %s\n", pnfft_gb300_last_error());
 }
 
 void pnfftf_adj(pnfftf_plan ths, pnfftf_nodes nodes, unsigned compute_flags) {
   if (!ths || !nodes) return;
-  const size_t M = (size_t)(nodes->M > 0 ? nodes->M : 0), tu = tuple(ths);
-  double *fh = (double *)pnfft_get_f_hat(ths->p);
-  if ((compute_flags & PNFFT_COMPUTE_ACCUMULATED) && ths->f_hat && fh)
-    to_double(fh, ths->f_hat, 2 * (size_t)ths->nfh);
-  stage_x(nodes);
-  double *sf = nullptr, *sg = nullptr;
-  if ((compute_flags & PNFFT_COMPUTE_F) && nodes->f) {
-    sf = staging(&nodes->sf, 2 * M);
-    to_double(sf, nodes->f, M * tu);
-  }
-  if ((compute_flags & PNFFT_COMPUTE_GRAD_F) && nodes->grad) {
-    sg = staging(&nodes->sgrad, 6 * M);
-    to_double(sg, nodes->grad, 3 * M * tu);
-  }
-  pnfft_set_f((pnfft_complex *)sf, nodes->nd);
-  pnfft_set_grad_f((pnfft_complex *)sg, nodes->nd);
-  pnfft_adj(ths->p, nodes->nd, compute_flags);
-  if (ths->f_hat && fh) to_float(ths->f_hat, fh, 2 * (size_t)ths->nfh);
+  if (pnfftf_gb300_adj_dev(ths, nodes, compute_flags)) fprintf(stderr, "pnfftf_adj: %s\n", pnfft_gb300_last_error());
 }
 
 // --- memory, generators ------------------------------------------------------------
