@@ -23,8 +23,8 @@ namespace pg {
 //   s_c = sum_p psi_z'[p] g_c[p]         (psi_z' zero outside the stencil)
 // The thread's share of the node's value is psi_x[a] (psi_y[b] s_0 +
 // psi_y[b + R/2] s_1); the shares of all threads are added in a fixed order
-// in shared memory (four threads per node, then two shuffles), so a node's
-// result depends only on the node.
+// in shared memory (four threads per node with compensated (Kahan) sums, then
+// two shuffles), so a node's result depends only on the node.
 // Window values: one thread per (axis, node) evaluates the node's CUT values
 // on that axis (a warp shares the axis, so the fitted polynomials'
 // coefficients are broadcast reads) into its row: the z row in slot rotation
@@ -249,10 +249,7 @@ __global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 4) k_interp_line(Con
     {
       const int i = tid >> 2, r = tid & 3;
       float2 s = make_float2(0.f, 0.f);
-      if (i < nb) {
-#pragma unroll 8
-        for (int k = r; k < NTH; k += 4) s = __fadd2_rn(s, s_part[i][k]);
-      }
+      if (i < nb) s = kahan_quarter_sum<NTH>(s_part[i], r);
       s.x += __shfl_xor_sync(0xffffffffu, s.x, 1);
       s.y += __shfl_xor_sync(0xffffffffu, s.y, 1);
       s.x += __shfl_xor_sync(0xffffffffu, s.x, 2);

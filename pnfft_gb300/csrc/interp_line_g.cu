@@ -20,7 +20,7 @@ namespace pg {
 //   d/dy = psi_x (dpsi_y0 s_0 + dpsi_y1 s_1)    d/dz = psi_x  (psi_y0 t_0 + psi_y1 t_1)
 // (psi' in grid units, as the reference's pre_dpsi_tensor).  The shares of
 // all threads are added in a fixed order in shared memory, four threads per
-// (node, output), in sub-batches of NS nodes (as many as the CTA's threads
+// (node, output) with compensated (Kahan) sums, in sub-batches of NS nodes (as many as the CTA's threads
 // cover).  Window rows (psi and psi' on
 // each axis) are evaluated for NB nodes at a time, one thread per (derivative,
 // axis, node), a warp sharing the polynomial rows.
@@ -246,10 +246,7 @@ __global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 3) k_interp_line_g(C
         const int o = pr / NS, k = pr - o * NS;
         float2 sum = make_float2(0.f, 0.f);
         const bool valid = pr < NO * NS && k < ns;
-        if (valid) {
-#pragma unroll 8
-          for (int q = r; q < NTH; q += 4) sum = __fadd2_rn(sum, s_part[pr][q]);
-        }
+        if (valid) sum = kahan_quarter_sum<NTH>(s_part[pr], r);
         sum.x += __shfl_xor_sync(0xffffffffu, sum.x, 1);
         sum.y += __shfl_xor_sync(0xffffffffu, sum.y, 1);
         sum.x += __shfl_xor_sync(0xffffffffu, sum.x, 2);
