@@ -11,8 +11,9 @@ are declared fixed, so the binning is computed once and reused. It can then
 pick each plan's convolution kernels by timing them (``autotune``: the line
 kernels, the FP32-mixed tile kernels and the one-thread-per-node kernels,
 which win for small M on large grids). Finally it captures all items
-on one stream into a single CUDA graph. ``run()`` replays the whole batch with
-one graph launch, so the per-call host work of the C library (argument
+into a single CUDA graph, the plans spread over a few concurrent branches
+(streams) so that small plans do not leave the GPU idle one after another.
+``run()`` replays the whole batch with one graph launch, so the per-call host work of the C library (argument
 checks, stream and pointer setup, about 50 launches per item) is paid once
 at capture.
 
@@ -27,10 +28,15 @@ __all__ = ["Batch"]
 
 
 class Batch:
-    def __init__(self, device=None):
+    """streams: the number of branches the plans are spread over (all items of
+    one plan stay on one branch, in the order they were added); branches run
+    concurrently, in eager runs and in the captured graph."""
+
+    def __init__(self, device=None, streams=4):
         self.items = []
         self.device = torch.device(device or "cuda")
         self.stream = torch.cuda.Stream(self.device)
+        self.side = [torch.cuda.Stream(self.device) for _ in range(max(1, int(streams)))]
         self.graph = None
         self.choice = {}
 
@@ -57,11 +63,41 @@ class Batch:
         else:
             plan.adj_device(x, f, grad, flags, f_hat=f_hat, fixed_nodes=True)
 
+    def _branches(self):
+        """The items split into one list per branch: plans by decreasing node
+        count, each to the branch with the fewest nodes so far."""
+        plans = self._plans()
+        load = [sum(int(it[2].shape[0]) for it in self.items if it[1] is p) for p in plans]
+        tot = [0] * len(self.side)
+        where = {}
+        for k in sorted(range(len(plans)), key=lambda k: -load[k]):
+            b = min(range(len(tot)), key=tot.__getitem__)
+            where[id(plans[k])] = b
+            tot[b] += load[k]
+        out = [[] for _ in self.side]
+        for it in self.items:
+            out[where[id(it[1])]].append(it)
+        return out
+
+    def _run_branches(self):
+        """Fork the branches from the batch stream, run each branch's items on
+        its stream, join them back."""
+        branches = self._branches()
+        for s, items in zip(self.side, branches):
+            if not items:
+                continue
+            s.wait_stream(self.stream)
+            with torch.cuda.stream(s):
+                for it in items:
+                    self._run_item(it)
+        for s, items in zip(self.side, branches):
+            if items:
+                self.stream.wait_stream(s)
+
     def run_eager(self):
-        """Run the items one by one on the batch stream (no graph)."""
-        with torch.cuda.stream(self.stream):
-            for it in self.items:
-                self._run_item(it)
+        """Run the items without a graph, the branches concurrently; ordered
+        after the work on the batch stream and before what follows on it."""
+        self._run_branches()
 
     def _time_plan(self, plan, reps):
         items = [it for it in self.items if it[1] is plan]
@@ -114,10 +150,10 @@ class Batch:
         self.run_eager()
         for p in self._plans():
             p.synchronize()  # also recycles the stage-timer events of the eager calls
+        self.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
-            for it in self.items:
-                self._run_item(it)
+            self._run_branches()
         self.graph = g
         return g
 
@@ -129,4 +165,6 @@ class Batch:
             self.graph.replay()
 
     def synchronize(self):
+        for s in self.side:
+            s.synchronize()
         self.stream.synchronize()
