@@ -477,9 +477,16 @@ def run_batched(P, torch, dev, steps=5):
     ms_graph = timed(batch.run)
     ms_eager = timed(batch.run_eager)
     branches = len(batch.side)
-    batch.side = batch.side[:1]  # the same graph with every plan on one stream
+    sides = batch.side
+    batch.side = sides[:1]  # the same graph with every plan on one stream
     batch.graph = None
     ms_graph_1 = timed(batch.run)
+    batch.side = sides
+    batch.fused = True  # one batched convolution launch per direction and cutoff
+    batch.graph = None
+    ms_fused = timed(batch.run)
+    fused_calls, fused_launches = batch.fused_stats()
+    ms_fused_eager = timed(batch.run_eager)
     nodes = batch.nodes()
     errs = []
     for N, m, x, fh, fo in checks:
@@ -491,6 +498,9 @@ def run_batched(P, torch, dev, steps=5):
     return {"value": nodes / (ms_graph * 1e-3) / 1e6, "unit": "Mpts/s", "ms_per_replay": ms_graph,
             "eager_value": nodes / (ms_eager * 1e-3) / 1e6, "eager_ms": ms_eager, "graph_branches": branches,
             "one_branch_value": nodes / (ms_graph_1 * 1e-3) / 1e6, "one_branch_ms": ms_graph_1,
+            "fused_value": nodes / (ms_fused * 1e-3) / 1e6, "fused_ms": ms_fused,
+            "fused_eager_value": nodes / (ms_fused_eager * 1e-3) / 1e6,
+            "fused_calls": fused_calls, "fused_launches": fused_launches,
             "plans": 65, "rhs_sharing_nodes": 8, "node_transforms_per_replay": nodes,
             "per_node_kernels_chosen": sum(1 for c in choice.values() if c[0] == 1),
             "tunings_chosen": _count_tunings(choice),

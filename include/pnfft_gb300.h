@@ -87,6 +87,27 @@ int pnfft_gb300_get_tuning(const pnfft_plan ths, int *tuning3);
  * in [32, 4096]), e.g. a tuning saved from an earlier run. */
 int pnfft_gb300_set_tuning(pnfft_plan ths, const int *tuning3);
 
+/* Batched convolutions (no counterpart in the reference).  Between
+ * pnfft_gb300_batch_begin(stream) and pnfft_gb300_batch_end(), every
+ * pnfft_trafo / pnfft_adj on that stream (pnfft_gb300_set_stream) with device
+ * arrays attached, fixed nodes, an FP32-mixed plan, COMPUTE_F alone, the
+ * line kernels (conv method 0; no ik, interlacing, gradient or Hessian) and
+ * fewer line sub-problems than 4 CTAs per SM (a call too small to fill the
+ * GPU alone; larger calls keep their grid in L2 from D to B) runs
+ * its binning and D + F (trafo) or binning and grid clearing (adjoint) at
+ * once, each into a grid of its own, and defers its convolution.
+ * pnfft_gb300_batch_end launches, per direction and cutoff, one kernel over
+ * the sub-problems of all deferred calls, then the adjoints' F^H and D^T, all
+ * on the stream, without synchronizing.  Other calls run as usual.  The calls
+ * of a batch must be independent: none may read an array another one writes.
+ * A batch can be captured into a CUDA graph after one uncaptured run of the
+ * same calls (which allocates the grids).  Returns 0 on success. */
+int pnfft_gb300_batch_begin(void *cuda_stream);
+int pnfft_gb300_batch_end(void);
+/* Of the last closed batch: the calls whose convolution was deferred, and
+ * the batched convolution kernels launched for them. */
+int pnfft_gb300_batch_stats(int *deferred_calls, int *launches);
+
 /* Zero-copy mode.  When device arrays are attached, pnfft_trafo/pnfft_adj read
  * and write them directly and return without synchronizing the stream; the
  * host pointers of the plan/nodes are not touched.  Layouts are those of the

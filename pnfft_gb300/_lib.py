@@ -177,6 +177,9 @@ SIGNATURES = {
     "pnfft_gb300_autotune": (_I, [_P, _P, _U, _U, _I]),
     "pnfft_gb300_get_tuning": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
     "pnfft_gb300_set_tuning": (_I, [_P, ctypes.POINTER(ctypes.c_int)]),
+    "pnfft_gb300_batch_begin": (_I, [_P]),
+    "pnfft_gb300_batch_end": (_I, []),
+    "pnfft_gb300_batch_stats": (_I, [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
 }
 
 _lib = None

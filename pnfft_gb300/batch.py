@@ -22,7 +22,7 @@ tensors in place between replays.
 """
 import torch
 
-from . import COMPUTE_F, Plan  # noqa: F401  (Plan for type references in docs)
+from . import COMPUTE_F, Plan, _check, _stream_handle, load  # noqa: F401  (Plan for type references in docs)
 
 __all__ = ["Batch"]
 
@@ -30,9 +30,14 @@ __all__ = ["Batch"]
 class Batch:
     """streams: the number of branches the plans are spread over (all items of
     one plan stay on one branch, in the order they were added); branches run
-    concurrently, in eager runs and in the captured graph."""
+    concurrently, in eager runs and in the captured graph.  fused: instead of
+    branches, all items on one stream inside a pnfft_gb300 batch, so that the
+    convolutions of all calls that qualify (FP32-mixed, f alone, line kernels)
+    run as one launch per direction and cutoff; the items must be
+    independent (no item reads what another writes)."""
 
-    def __init__(self, device=None, streams=4):
+    def __init__(self, device=None, streams=4, fused=False):
+        self.fused = bool(fused)
         self.items = []
         self.device = torch.device(device or "cuda")
         self.stream = torch.cuda.Stream(self.device)
@@ -94,10 +99,39 @@ class Batch:
             if items:
                 self.stream.wait_stream(s)
 
+    def _run_fused(self):
+        """All items on the batch stream inside pnfft_gb300_batch_begin / _end:
+        the FP32-mixed f-only line convolutions of all plans run as one launch
+        per direction and cutoff."""
+        L = load()
+        with torch.cuda.stream(self.stream):
+            L.pnfft_gb300_clear_error()
+            _check(L.pnfft_gb300_batch_begin(_stream_handle(self.stream)), "pnfft_gb300_batch_begin")
+            try:
+                for it in self.items:
+                    self._run_item(it)
+            finally:
+                rc = L.pnfft_gb300_batch_end()
+            _check(rc, "pnfft_gb300_batch_end")
+
+    def fused_stats(self):
+        """(calls deferred, batched convolution launches) of the last fused run."""
+        import ctypes
+        a, b = ctypes.c_int(0), ctypes.c_int(0)
+        _check(load().pnfft_gb300_batch_stats(ctypes.byref(a), ctypes.byref(b)), "pnfft_gb300_batch_stats")
+        return a.value, b.value
+
+    def _run_all(self):
+        if self.fused:
+            self._run_fused()
+        else:
+            self._run_branches()
+
     def run_eager(self):
-        """Run the items without a graph, the branches concurrently; ordered
-        after the work on the batch stream and before what follows on it."""
-        self._run_branches()
+        """Run the items without a graph (branches concurrently, or fused);
+        ordered after the work on the batch stream and before what follows on
+        it."""
+        self._run_all()
 
     def _time_plan(self, plan, reps):
         items = [it for it in self.items if it[1] is plan]
@@ -153,7 +187,7 @@ class Batch:
         self.synchronize()
         g = torch.cuda.CUDAGraph()
         with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
-            self._run_branches()
+            self._run_all()
         self.graph = g
         return g
 

@@ -960,6 +960,13 @@ extern "C" int pnfft_gb300_autotune(pnfft_plan ths, pnfft_nodes nodes, unsigned 
   }
   return engine_autotune(ths, nodes, trafo_flags, adj_flags, reps > 0 ? reps : 2);
 }
+extern "C" int pnfft_gb300_batch_begin(void *stream) { return engine_batch_begin(stream); }
+extern "C" int pnfft_gb300_batch_end(void) { return engine_batch_end(); }
+extern "C" int pnfft_gb300_batch_stats(int *deferred_calls, int *launches) {
+  if (!deferred_calls || !launches) return -1;
+  engine_batch_stats(deferred_calls, launches);
+  return 0;
+}
 extern "C" int pnfft_gb300_get_conv_kernel(const pnfft_plan ths, int adjoint) {
   return ths ? ths->last_conv[adjoint ? 1 : 0] : -1;
 }

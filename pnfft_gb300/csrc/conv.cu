@@ -329,6 +329,24 @@ static bool tiles_usable(const ConvArgs &a) {
   return a.w.cut <= 15 && a.bin.T[0] == 8 && a.bin.T[1] == 8 && a.bin.T[2] == 8;
 }
 
+bool interp_line_chosen(const ConvArgs &a, int mode, bool fp32) {
+  const int c = a.w.cut;
+  return a.M > 0 && fp32 && mode == 1 && a.method == 0 && a.bin.line_mode == BIN_LINE && tiles_usable(a) &&
+         (c == 5 || c == 7 || c == 9 || c == 11 || c == 13);
+}
+
+bool spread_line_f_chosen(const ConvArgs &a, int mode, bool fp32) {
+  const int c = a.w.cut;
+  return a.M > 0 && fp32 && mode == 1 && a.method == 0 && a.bin.line_mode == BIN_LINE && tiles_usable(a) &&
+         (c == 5 || c == 7 || c == 9 || c == 11 || c == 13);
+}
+
+__global__ void k_store_conv_args(ConvArgs a, ConvArgs *dst) {
+  if (threadIdx.x == 0) *dst = a;
+}
+
+void store_conv_args(const ConvArgs &a, ConvArgs *dst, cudaStream_t s) { k_store_conv_args<<<1, 32, 0, s>>>(a, dst); }
+
 int launch_interp(const ConvArgs &a, int mode, bool fp32, cudaStream_t s) {
   if (a.M == 0) return CONV_NONE;
   if (fp32 && mode == 1 && a.method == 0 && a.bin.line_mode == BIN_LINE && tiles_usable(a) &&

@@ -70,6 +70,13 @@ struct DevState {
   std::vector<Stage> pending;
   bool capturing = false;  // the current call is being captured into a CUDA graph
   std::vector<cudaEvent_t> free_ev;
+  // batched convolutions (pnfft_gb300_batch_begin / _end): the k-th deferred
+  // call of this plan in an open batch uses grid bgrid[k] and keeps its
+  // arguments in bargs[k]; both stay allocated for later batches and graph
+  // replays
+  std::vector<void *> bgrid;
+  std::vector<ConvArgs *> bargs;
+  int bslot = 0;  // deferred calls of this plan in the open batch
 };
 
 // A binning of a node set onto grid tiles, kept with the node set: one slot
@@ -324,19 +331,189 @@ static NodeDev *node_dev(pnfft_nodes nd) {
   return nd->dev;
 }
 
+// ---------------------------------------------------------------------------
+// batched convolutions
+//
+// Between pnfft_gb300_batch_begin(stream) and pnfft_gb300_batch_end(), a call
+// on that stream with device arrays, fixed nodes and an FP32-mixed f-only
+// line convolution (no ik, interlacing, gradient or Hessian) too small to
+// fill the GPU alone runs its binning
+// and D + F (trafo) or its binning and grid clearing (adjoint) at once into a
+// grid of its own, and defers B or B^T.  The end of the batch launches one
+// kernel per direction and cutoff over the line sub-problems of all deferred
+// calls (up to kMultiItems per launch), then the adjoints' F^H and D^T.  The
+// calls of a batch must be independent (none reads what another writes).
+// ---------------------------------------------------------------------------
+struct Deferred {
+  pnfft_plan p;
+  BinSlot *slot;          // the node set's binning the call reads
+  int adjoint, cut, max_subs;
+  const ConvArgs *dargs;  // the call's arguments in device memory
+  void *grid;
+  DeconvArgs da;          // adjoint: D^T after F^H on `grid`
+};
+
+struct BatchState {
+  bool active = false;
+  cudaStream_t s = nullptr;
+  std::vector<Deferred> items;
+  std::vector<pnfft_plan> plans;  // plans with deferred calls
+  int deferred = 0;               // calls deferred since the batch opened
+  int launches = 0;               // batched kernel launches since the batch opened
+  int last_deferred = 0, last_launches = 0;  // of the last closed batch
+  cudaEvent_t ev = nullptr;       // orders a rebinning after an early flush
+};
+static BatchState g_batch;
+
+static int fft_exec_on(pnfft_plan p, void *grid, int direction) {
+  DevState *d = p->dev;
+  if (fp32(p)) PG_FFT(cufftExecC2C(d->fft, (cufftComplex *)grid, (cufftComplex *)grid, direction));
+  else PG_FFT(cufftExecZ2Z(d->fft, (cufftDoubleComplex *)grid, (cufftDoubleComplex *)grid, direction));
+  return 0;
+}
+
+// Only calls too small to fill the GPU alone are deferred (fewer line
+// sub-problems than 4 CTAs per SM): a large call keeps D, F and B back to
+// back on one grid, which stays in L2, and fills the GPU by itself.
+static bool batch_small(const Binning &b) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+  }
+  return b.max_subs < 4 * sms;
+}
+
+// the grid and argument slot of the plan's next deferred call; false (the
+// call then runs as usual) where a slot would need an allocation during a
+// stream capture or the allocation fails
+static bool batch_slot(pnfft_plan p, void **grid, ConvArgs **dargs) {
+  DevState *d = p->dev;
+  const int k = d->bslot;
+  if (k >= (int)d->bgrid.size() || k >= (int)d->bargs.size()) {
+    if (d->capturing) return false;
+    void *g = nullptr;
+    ConvArgs *a = nullptr;
+    if (cudaMalloc(&g, d->grid_bytes) != cudaSuccess || cudaMalloc(&a, sizeof(ConvArgs)) != cudaSuccess) {
+      cudaGetLastError();
+      if (g) cudaFree(g);
+      return false;
+    }
+    d->bgrid.push_back(g);
+    d->bargs.push_back(a);
+  }
+  *grid = d->bgrid[k];
+  *dargs = d->bargs[k];
+  if (d->bslot++ == 0) g_batch.plans.push_back(p);
+  return true;
+}
+
+static int batch_flush() {
+  if (g_batch.items.empty()) return 0;
+  const cudaStream_t s = g_batch.s;
+  std::vector<Deferred> &items = g_batch.items;
+  for (int adj = 0; adj < 2; adj++) {
+    std::vector<int> cuts;
+    for (const Deferred &it : items)
+      if (it.adjoint == adj && std::find(cuts.begin(), cuts.end(), it.cut) == cuts.end()) cuts.push_back(it.cut);
+    for (int cut : cuts) {
+      MultiConv mc;
+      memset(&mc, 0, sizeof(mc));
+      auto launch = [&]() -> bool {
+        const bool ok = adj ? launch_spread_line_f_multi(mc, cut, s) : launch_interp_line_multi(mc, cut, s);
+        g_batch.launches++;
+        mc.n = 0;
+        mc.first[0] = 0;
+        return ok;
+      };
+      for (const Deferred &it : items) {
+        if (it.adjoint != adj || it.cut != cut) continue;
+        mc.args[mc.n] = it.dargs;
+        mc.first[mc.n + 1] = mc.first[mc.n] + it.max_subs;
+        mc.n++;
+        if (mc.n == kMultiItems && !launch()) return set_error("batched convolution: no kernel for cutoff %d", cut), -1;
+      }
+      if (mc.n > 0 && !launch()) return set_error("batched convolution: no kernel for cutoff %d", cut), -1;
+    }
+  }
+  for (const Deferred &it : items) {
+    if (!it.adjoint) continue;
+    DevState *d = it.p->dev;
+    PG_FFT(cufftSetStream(d->fft, s));
+    const int rc = fft_exec_on(it.p, it.grid, CUFFT_INVERSE);
+    PG_FFT(cufftSetStream(d->fft, d->stream));
+    if (rc) return -1;
+    launch_deconv_crop_acc(it.da, fp32(it.p), s);
+  }
+  PG_CUDA(cudaGetLastError());
+  for (pnfft_plan p : g_batch.plans)
+    if (p->dev) p->dev->bslot = 0;
+  items.clear();
+  g_batch.plans.clear();
+  return 0;
+}
+
+int engine_batch_begin(void *stream) {
+  if (g_batch.active) return set_error("pnfft_gb300_batch_begin: a batch is already open"), -1;
+  if (!stream) return set_error("pnfft_gb300_batch_begin: a stream is required"), -1;
+  g_batch.active = true;
+  g_batch.s = (cudaStream_t)stream;
+  g_batch.deferred = g_batch.launches = 0;
+  g_batch.items.clear();
+  g_batch.plans.clear();
+  return 0;
+}
+
+int engine_batch_end() {
+  if (!g_batch.active) return set_error("pnfft_gb300_batch_end: no batch is open"), -1;
+  const int rc = batch_flush();
+  g_batch.active = false;
+  g_batch.last_deferred = g_batch.deferred;
+  g_batch.last_launches = g_batch.launches;
+  g_batch.items.clear();
+  for (pnfft_plan p : g_batch.plans)
+    if (p->dev) p->dev->bslot = 0;
+  g_batch.plans.clear();
+  return rc;
+}
+
+void engine_batch_stats(int *deferred, int *launches) {
+  *deferred = g_batch.last_deferred;
+  *launches = g_batch.last_launches;
+}
+
+static bool batch_uses_slot(const BinSlot *sl) {
+  for (const Deferred &it : g_batch.items)
+    if (it.slot == sl) return true;
+  return false;
+}
+
 // the binning slot of these nodes for pass `il` of a B (spread = 0) or B^T
 // (spread = 1), (re)allocated for the plan's tile shape when needed
+// the slot a binning of these nodes goes to, and whether its allocation
+// already fits the plan's tile shape, sub-problem size and precision
+static BinSlot *binning_target(pnfft_plan p, pnfft_nodes nd, int spread, int il, bool f_only, int *T,
+                               int *line_mode, int *sub_max, bool *fits) {
+  const int64_t M = nd->local_M;
+  int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
+  choose_tiles(p->cutoff, fp32(p), spread != 0, f_only, p->conv_method[spread ? 1 : 0], n, M, T, line_mode);
+  BinSlot &sl = node_dev(nd)->bins[*line_mode == BIN_LINE ? 0 : 1][il];
+  *sub_max = *line_mode == BIN_LINE ? p->line_sub_max : 1024;
+  bool same = T[0] == sl.T[0] && T[1] == sl.T[1] && T[2] == sl.T[2] && *line_mode == sl.line_mode &&
+              sl.b.sub_max == *sub_max;
+  for (int t = 0; t < 3; t++) same = same && sl.b.ntile[t] == (n[t] + T[t] - 1) / T[t];
+  *fits = same && sl.cap >= M && sl.b.key && sl.prec == p->precision;
+  return &sl;
+}
+
 static BinSlot *ensure_binning(pnfft_plan p, pnfft_nodes nd, int spread, int il, bool f_only) {
   const int64_t M = nd->local_M;
   int n[3] = {(int)p->n[0], (int)p->n[1], (int)p->n[2]};
-  int T[3], line_mode = 0;
-  choose_tiles(p->cutoff, fp32(p), spread != 0, f_only, p->conv_method[spread ? 1 : 0], n, M, T, &line_mode);
-  BinSlot &sl = node_dev(nd)->bins[line_mode == BIN_LINE ? 0 : 1][il];
-  const int sub_max = line_mode == BIN_LINE ? p->line_sub_max : 1024;
-  bool same = T[0] == sl.T[0] && T[1] == sl.T[1] && T[2] == sl.T[2] && line_mode == sl.line_mode &&
-              sl.b.sub_max == sub_max;
-  for (int t = 0; t < 3; t++) same = same && sl.b.ntile[t] == (n[t] + T[t] - 1) / T[t];
-  if (same && sl.cap >= M && sl.b.key && sl.prec == p->precision) return &sl;
+  int T[3], line_mode = 0, sub_max = 0;
+  bool fits = false;
+  BinSlot &sl = *binning_target(p, nd, spread, il, f_only, T, &line_mode, &sub_max, &fits);
+  if (fits) return &sl;
   int64_t cap = std::max<int64_t>(M, std::max<int64_t>(sl.cap, 1));
   Binning &b = sl.b;
   free_binning(b);
@@ -525,6 +702,22 @@ static int fft_exec(pnfft_plan p, int direction) {
 static int do_binning(pnfft_plan p, pnfft_nodes nd, ConvArgs &a, int il, int adj, cudaStream_t s, bool f_only) {
   DevState *d = p->dev;
   if (!s) s = d->stream;
+  if (!g_batch.items.empty()) {
+    // a deferred call of the open batch reads this slot: run the batch before
+    // the slot is reallocated or rebinned
+    int T[3], lm = 0, sm = 0;
+    bool fits = false;
+    BinSlot *t = binning_target(p, nd, adj, il, f_only, T, &lm, &sm, &fits);
+    const bool reuse = fits && nd->fixed && t->valid && t->plan == p->uid && t->ver == nd->version;
+    if (!reuse && batch_uses_slot(t)) {
+      if (batch_flush()) return -1;
+      // the flushed kernels read the slot on the batch stream: the binning
+      // below, on its own stream, waits for them
+      if (!g_batch.ev) PG_CUDA(cudaEventCreateWithFlags(&g_batch.ev, cudaEventDisableTiming));
+      PG_CUDA(cudaEventRecord(g_batch.ev, g_batch.s));
+      PG_CUDA(cudaStreamWaitEvent(s, g_batch.ev, 0));
+    }
+  }
   BinSlot *sl = ensure_binning(p, nd, adj, il, f_only);
   if (!sl) return -1;
   a.bin = sl->b;
@@ -762,6 +955,20 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
           pass_bin[pass] = ca.bin;
         }
       }
+      // an open batch defers B: D and F go to the call's own grid
+      void *bgrid = nullptr;
+      ConvArgs *bdargs = nullptr;
+      bool defer = false;
+      if (g_batch.active && zc && fork && !il_plan && !ik && nd->fixed && s == g_batch.s && (cflags & C_F) &&
+          !(cflags & (C_GRAD | C_HESS | PNFFT_OMIT_CONV | PNFFT_OMIT_FFT | PNFFT_OMIT_DECONV))) {
+        ConvArgs probe = ca;
+        probe.bin = pass_bin[0];
+        defer = interp_line_chosen(probe, 1, f32) && batch_small(probe.bin) && batch_slot(p, &bgrid, &bdargs);
+      }
+      if (defer) {
+        ca.grid = bgrid;
+        da.grid = bgrid;
+      }
       for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
         const int il = il_plan ? pass : 0;
         ca.use_il = il_plan ? 1 : 0;
@@ -812,7 +1019,9 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
           }
           {
             StageScope sc(d, PNFFT_TIMER_MATRIX_F, 0);
-            if (!(cflags & PNFFT_OMIT_FFT) && fft_exec(p, CUFFT_FORWARD)) return -1;
+            if (!(cflags & PNFFT_OMIT_FFT) &&
+                (defer ? fft_exec_on(p, bgrid, CUFFT_FORWARD) : fft_exec(p, CUFFT_FORWARD)))
+              return -1;
           }
           if (!(cflags & PNFFT_OMIT_CONV) && nd) {
             if (fj.pending) PG_CUDA(fj.join());
@@ -823,9 +1032,25 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
             c.f_out = A.f;
             c.grad_out = A.grad;
             c.hess_out = A.hess;
-            int mode = ((cflags & C_F) ? 1 : 0) | ((cflags & C_GRAD) ? 2 : 0);
-            if (mode) p->last_conv[0] = launch_interp(c, mode, f32, s);
-            if (cflags & C_HESS) p->last_conv[0] = launch_interp(c, 4, f32, s);
+            if (defer) {
+              store_conv_args(c, bdargs, s);
+              Deferred it;
+              memset(&it, 0, sizeof(it));
+              it.p = p;
+              it.slot = &node_dev(nd)->bins[0][0];
+              it.adjoint = 0;
+              it.cut = p->cutoff;
+              it.max_subs = c.bin.max_subs;
+              it.dargs = bdargs;
+              it.grid = bgrid;
+              g_batch.items.push_back(it);
+              g_batch.deferred++;
+              p->last_conv[0] = CONV_LINE;
+            } else {
+              int mode = ((cflags & C_F) ? 1 : 0) | ((cflags & C_GRAD) ? 2 : 0);
+              if (mode) p->last_conv[0] = launch_interp(c, mode, f32, s);
+              if (cflags & C_HESS) p->last_conv[0] = launch_interp(c, 4, f32, s);
+            }
           }
         }
       }
@@ -920,6 +1145,16 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
           pass_bin[pass] = ca.bin;
         }
       }
+      // an open batch defers B^T, and F^H and D^T after it, on the call's own grid
+      void *bgrid = nullptr;
+      ConvArgs *bdargs = nullptr;
+      bool defer = false;
+      if (g_batch.active && zc && fork && !il_plan && !ik && nd->fixed && s == g_batch.s && (cflags & C_F) &&
+          !(cflags & (C_GRAD | PNFFT_OMIT_CONV | PNFFT_OMIT_FFT | PNFFT_OMIT_DECONV))) {
+        ConvArgs probe = ca;
+        probe.bin = pass_bin[0];
+        defer = spread_line_f_chosen(probe, 1, f32) && batch_small(probe.bin) && batch_slot(p, &bgrid, &bdargs);
+      }
       for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
         const int il = il_plan ? pass : 0;
         ca.use_il = il_plan ? 1 : 0;
@@ -928,6 +1163,34 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
         ca.bin = pass_bin[pass];
         auto one = [&](int ikmode, int ikdim, const double *fin, const double *gin, int64_t off, int64_t stride,
                        int mode) -> int {
+          if (defer) {
+            PG_CUDA(cudaMemsetAsync(bgrid, 0, gbytes, s));
+            if (fj.pending) PG_CUDA(fj.join());
+            ConvArgs c = ca;
+            c.grid = bgrid;
+            c.offset = off;
+            c.stride = stride;
+            c.f_in = fin;
+            c.grad_in = gin;
+            store_conv_args(c, bdargs, s);
+            Deferred it;
+            memset(&it, 0, sizeof(it));
+            it.p = p;
+            it.slot = &node_dev(nd)->bins[0][0];
+            it.adjoint = 1;
+            it.cut = p->cutoff;
+            it.max_subs = c.bin.max_subs;
+            it.dargs = bdargs;
+            it.grid = bgrid;
+            it.da = da;
+            it.da.grid = bgrid;
+            it.da.ik = ikmode;
+            it.da.ik_dim = ikdim;
+            g_batch.items.push_back(it);
+            g_batch.deferred++;
+            p->last_conv[1] = CONV_LINE;
+            return 0;
+          }
           PG_CUDA(cudaMemsetAsync(d->grid, 0, gbytes, s));
           if (fj.pending) PG_CUDA(fj.join());  // B^T needs the binning from the auxiliary stream
           {
@@ -1195,8 +1458,16 @@ int engine_sync(pnfft_plan p) {
 void engine_release_plan(pnfft_plan p) {
   DevState *d = p->dev;
   if (!d) return;
+  for (const Deferred &it : g_batch.items)
+    if (it.p == p) {
+      batch_flush();  // the plan's deferred calls run before its buffers go
+      break;
+    }
+  g_batch.plans.erase(std::remove(g_batch.plans.begin(), g_batch.plans.end(), p), g_batch.plans.end());
   if (d->device >= 0) {
     cudaStreamSynchronize(d->stream);
+    for (void *g : d->bgrid) cudaFree(g);  // cudaFree waits for the device
+    for (ConvArgs *a : d->bargs) cudaFree(a);
     d->pending.clear();
     if (d->grid) cudaFree(d->grid);
     if (d->fft_prec >= 0) cufftDestroy(d->fft);

@@ -95,7 +95,7 @@ __device__ __forceinline__ float2 share(const float *row, int ca, int cb, float2
 }
 
 template <int CUT>
-__global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 4) k_interp_line(ConvArgs a) {
+__device__ __forceinline__ void interp_line_body(const ConvArgs &a, const int sub) {
   typedef LineGeom32<CUT> G;
   constexpr int TL = G::TL, R = G::R, HR = G::HR, W = G::W, NG = G::NG, NB = G::NB, WS = G::WS, PS = G::PS,
                 PR = G::PR, NTH = G::THREADS;
@@ -107,7 +107,6 @@ __global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 4) k_interp_line(Con
   __shared__ float s_d[NB][3];
   __shared__ int s_o[NB], s_j[NB], s_slab[NB];
   const Binning &b = a.bin;
-  const int sub = blockIdx.x;
   if (sub >= *b.nsub) return;
   const int line = b.sub_tile[sub], first = b.sub_first[sub], cnt = b.sub_cnt[sub];
   if (cnt <= 0) return;  // a line without nodes
@@ -278,8 +277,38 @@ __global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 4) k_interp_line(Con
 }
 
 template <int CUT>
+__global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 4) k_interp_line(ConvArgs a) {
+  interp_line_body<CUT>(a, blockIdx.x);
+}
+
+// the sub-problems of several calls of one cutoff in one launch
+template <int CUT>
+__global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 4) k_interp_line_multi(MultiConv mc) {
+  __shared__ __align__(16) ConvArgs s_args;
+  const int item = multi_item(mc, blockIdx.x);
+  copy_args(&s_args, mc.args[item]);
+  interp_line_body<CUT>(s_args, blockIdx.x - mc.first[item]);
+}
+
+template <int CUT>
 static void run_interp_line(const ConvArgs &a, cudaStream_t s) {
   k_interp_line<CUT><<<a.bin.max_subs, LineGeom32<CUT>::THREADS, 0, s>>>(a);
+}
+
+template <int CUT>
+static void run_interp_line_multi(const MultiConv &mc, cudaStream_t s) {
+  if (mc.first[mc.n] > 0) k_interp_line_multi<CUT><<<mc.first[mc.n], LineGeom32<CUT>::THREADS, 0, s>>>(mc);
+}
+
+bool launch_interp_line_multi(const MultiConv &mc, int cut, cudaStream_t s) {
+  switch (cut) {
+    case 5: run_interp_line_multi<5>(mc, s); return true;
+    case 7: run_interp_line_multi<7>(mc, s); return true;
+    case 9: run_interp_line_multi<9>(mc, s); return true;
+    case 11: run_interp_line_multi<11>(mc, s); return true;
+    case 13: run_interp_line_multi<13>(mc, s); return true;
+    default: return false;
+  }
 }
 
 bool launch_interp_line(const ConvArgs &a, cudaStream_t s) {

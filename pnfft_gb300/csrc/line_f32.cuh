@@ -108,4 +108,24 @@ __device__ __forceinline__ float2 kahan_quarter_sum(const float2 *part, int r) {
   return __fadd2_rn(s, make_float2(-c.x, -c.y));
 }
 
+// The item and sub-problem of block `blk` of a MultiConv launch, and a copy of
+// the item's arguments in shared memory (all threads of the block).
+__device__ __forceinline__ int multi_item(const MultiConv &mc, int blk) {
+  int lo = 0, hi = mc.n - 1;  // the last item with first[item] <= blk
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (mc.first[mid] <= blk) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void copy_args(ConvArgs *dst, const ConvArgs *src) {
+  static_assert(sizeof(ConvArgs) % 8 == 0, "ConvArgs copied in 8-byte words");
+  const unsigned long long *s = (const unsigned long long *)src;
+  unsigned long long *d = (unsigned long long *)dst;
+  for (int i = threadIdx.x; i < (int)(sizeof(ConvArgs) / 8); i += blockDim.x) d[i] = s[i];
+  __syncthreads();
+}
+
 }  // namespace pg

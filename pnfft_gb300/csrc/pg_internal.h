@@ -76,6 +76,9 @@ int engine_autotune(pnfft_plan ths, pnfft_nodes nodes, unsigned trafo_flags, uns
 int engine_charge_dipole(pnfft_plan ths, pnfft_nodes charges, pnfft_nodes dipoles, unsigned cflags, void *energy,
                          void *force);
 int engine_set_stream(pnfft_plan ths, void *stream);
+int engine_batch_begin(void *stream);
+int engine_batch_end();
+void engine_batch_stats(int *deferred, int *launches);
 int engine_sync(pnfft_plan ths);
 void engine_release_plan(pnfft_plan ths);
 void engine_release_nodes(pnfft_nodes nodes);

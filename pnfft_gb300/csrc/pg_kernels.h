@@ -94,6 +94,18 @@ struct ConvArgs {
   Binning bin;
 };
 
+// One launch over the line sub-problems of several calls (batched
+// convolutions, engine.cu): block k runs sub-problem k - first[i] of item i,
+// first[i] <= k < first[i + 1]; each item's ConvArgs sits in device memory
+// (written on the stream by store_conv_args) so that a captured graph replays
+// the same arguments.
+constexpr int kMultiItems = 64;
+struct MultiConv {
+  const ConvArgs *args[kMultiItems];
+  int first[kMultiItems + 1];
+  int n;
+};
+
 // Launchers (conv.cu).  `fp32` selects the FP32-mixed kernels.  `mode` is a
 // bit set of 1 = f, 2 = grad, 4 = hessian (interp) / 1 = f, 2 = grad (spread).
 // launch_interp / launch_spread return the ConvKernel family they launched.
@@ -114,6 +126,16 @@ bool launch_interp_tile_f32(const ConvArgs &a, int mode, cudaStream_t s);
 bool launch_interp_tile_f64(const ConvArgs &a, int mode, cudaStream_t s);
 // FP32-mixed f-only spreading on a BIN_LINE binning (spread_line_f.cu)
 bool launch_spread_line_f(const ConvArgs &a, cudaStream_t s);
+// the same kernels of one cutoff over the items of a MultiConv (first[n] blocks)
+bool launch_interp_line_multi(const MultiConv &mc, int cut, cudaStream_t s);
+bool launch_spread_line_f_multi(const MultiConv &mc, int cut, cudaStream_t s);
+// whether launch_interp / launch_spread would take k_interp_line /
+// k_spread_line_f for these arguments
+bool interp_line_chosen(const ConvArgs &a, int mode, bool fp32);
+bool spread_line_f_chosen(const ConvArgs &a, int mode, bool fp32);
+// copies `a` to device memory `dst` in stream order (a kernel with `a` as its
+// parameter, so that graph replays write the captured arguments)
+void store_conv_args(const ConvArgs &a, ConvArgs *dst, cudaStream_t s);
 // lines of tiles (spread_line_f32.cu, spread_line_f64.cu)
 bool launch_spread_line_f32(const ConvArgs &a, int mode, cudaStream_t s);
 bool launch_spread_line_f64(const ConvArgs &a, int mode, cudaStream_t s);

@@ -52,7 +52,7 @@ __device__ __forceinline__ void commit_z4(float2 *col, int z0, int n2, bool vec,
 }
 
 template <int CUT>
-__global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, CUT == 11 ? 3 : 4) k_spread_line_f(ConvArgs a) {
+__device__ __forceinline__ void spread_line_f_body(const ConvArgs &a, const int sub) {
   typedef LineGeom32<CUT> G;
   constexpr int TL = G::TL, R = G::R, HR = G::HR, W = G::W, NG = G::NG, PS = G::PS, NTH = G::THREADS;
   constexpr int NB = SpreadGeom32<CUT>::NB, WS = SpreadGeom32<CUT>::WS;
@@ -63,7 +63,6 @@ __global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, CUT == 11 ? 3 : 4) k
   __shared__ float2 s_f[NB];
   __shared__ int s_o[NB], s_slab[NB];
   const Binning &b = a.bin;
-  const int sub = blockIdx.x;
   if (sub >= *b.nsub) return;
   const int line = b.sub_tile[sub], first = b.sub_first[sub], cnt = b.sub_cnt[sub];
   if (cnt <= 0) return;  // a line without nodes
@@ -198,8 +197,38 @@ __global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, CUT == 11 ? 3 : 4) k
 }
 
 template <int CUT>
+__global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, CUT == 11 ? 3 : 4) k_spread_line_f(ConvArgs a) {
+  spread_line_f_body<CUT>(a, blockIdx.x);
+}
+
+// the sub-problems of several calls of one cutoff in one launch
+template <int CUT>
+__global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, CUT == 11 ? 3 : 4) k_spread_line_f_multi(MultiConv mc) {
+  __shared__ __align__(16) ConvArgs s_args;
+  const int item = multi_item(mc, blockIdx.x);
+  copy_args(&s_args, mc.args[item]);
+  spread_line_f_body<CUT>(s_args, blockIdx.x - mc.first[item]);
+}
+
+template <int CUT>
 static void run_spread_line_f(const ConvArgs &a, cudaStream_t s) {
   k_spread_line_f<CUT><<<a.bin.max_subs, LineGeom32<CUT>::THREADS, 0, s>>>(a);
+}
+
+template <int CUT>
+static void run_spread_line_f_multi(const MultiConv &mc, cudaStream_t s) {
+  if (mc.first[mc.n] > 0) k_spread_line_f_multi<CUT><<<mc.first[mc.n], LineGeom32<CUT>::THREADS, 0, s>>>(mc);
+}
+
+bool launch_spread_line_f_multi(const MultiConv &mc, int cut, cudaStream_t s) {
+  switch (cut) {
+    case 5: run_spread_line_f_multi<5>(mc, s); return true;
+    case 7: run_spread_line_f_multi<7>(mc, s); return true;
+    case 9: run_spread_line_f_multi<9>(mc, s); return true;
+    case 11: run_spread_line_f_multi<11>(mc, s); return true;
+    case 13: run_spread_line_f_multi<13>(mc, s); return true;
+    default: return false;
+  }
 }
 
 bool launch_spread_line_f(const ConvArgs &a, cudaStream_t s) {

@@ -92,3 +92,93 @@ def test_capture_refuses_host_arrays(lib):
     L.pnfft_gb300_set_stream(p.handle, None)
     f, _, _ = p.trafo(x, fh)  # the plan still works afterwards
     assert np.isfinite(f).all()
+
+
+def test_fused_batch_matches_separate_calls(lib, oracle):
+    """pnfft_gb300_batch_begin / _end (Batch(fused=True)): the f-only FP32
+    line convolutions of plans with cutoffs 9, 11 and 13 and of 3 right-hand
+    sides on one node set run as one launch per direction and cutoff; the
+    FP64 plan and the gradient trafo run as usual inside the same batch.
+    Interpolation results equal the separate calls bit for bit (a node's sum
+    has a fixed order); spreading results agree to FP32 rounding, and both
+    match the oracle.  The captured graph of the fused batch replays them."""
+    torch = pytest.importorskip("torch")
+    if lib.device_count() == 0:
+        pytest.fail("no CUDA device visible for a -m gpu test")
+    from pnfft_gb300.batch import Batch
+    rng = np.random.default_rng(61)
+    dev = "cuda"
+    specs = [((16, 16, 16), 3000, 4, "fp32"), ((16, 32, 16), 800, 5, "fp32"), ((32, 32, 32), 20000, 6, "fp32"),
+             ((16, 16, 16), 700, 4, "fp64")]
+    batch = Batch(fused=True)
+    ref = []
+    for N, M, m, prec in specs:
+        p = lib.Plan(N, m=m, precision=prec)
+        x = torch.tensor(rng.uniform(-0.5, 0.5, (M, 3)), device=dev)
+        S = int(np.prod(N))
+        fh = torch.tensor(rng.standard_normal(S) + 1j * rng.standard_normal(S), device=dev)
+        f_in = torch.tensor(rng.standard_normal(M) + 1j * rng.standard_normal(M), device=dev)
+        f_out = torch.zeros(M, dtype=torch.complex128, device=dev)
+        fh_out = torch.zeros(S, dtype=torch.complex128, device=dev)
+        batch.add_trafo(p, x, fh, f_out)
+        batch.add_adj(p, x, f_in, fh_out)
+        ref.append((p, N, m, prec, x, fh, f_in, f_out, fh_out))
+    # a gradient trafo (not deferred) and K = 3 right-hand sides on one node set
+    pg = lib.Plan((16, 16, 16), m=5, precision="fp32")
+    xg = torch.tensor(rng.uniform(-0.5, 0.5, (1500, 3)), device=dev)
+    fhg = torch.tensor(rng.standard_normal(4096) + 1j * rng.standard_normal(4096), device=dev)
+    fg = torch.zeros(1500, dtype=torch.complex128, device=dev)
+    gg = torch.zeros(1500, 3, dtype=torch.complex128, device=dev)
+    batch.add_trafo(pg, xg, fhg, fg, lib.COMPUTE_F | lib.COMPUTE_GRAD_F, grad=gg)
+    pk = lib.Plan((16, 16, 16), m=6, precision="fp32")
+    xk = torch.tensor(rng.uniform(-0.5, 0.5, (4000, 3)), device=dev)
+    rhs = []
+    for _ in range(3):
+        fh = torch.tensor(rng.standard_normal(4096) + 1j * rng.standard_normal(4096), device=dev)
+        fo = torch.zeros(4000, dtype=torch.complex128, device=dev)
+        batch.add_trafo(pk, xk, fh, fo)
+        rhs.append((fh, fo))
+    batch.run_eager()
+    batch.synchronize()
+    deferred, launches = batch.fused_stats()
+    assert deferred == 3 * 2 + 3  # three FP32 plans x (trafo, adj) + the three right-hand sides
+    assert launches == 3 + 3      # cutoffs 9, 11, 13 for B; 9, 11, 13 for B^T
+    # the same calls one by one, outside any batch
+    for p, N, m, prec, x, fh, f_in, f_out, fh_out in ref:
+        f_sep, _, _ = p.trafo_device(x, fh, lib.COMPUTE_F)
+        fh_sep = p.adj_device(x, f_in)
+        torch.cuda.synchronize()
+        o = oracle.OraclePlan(N, m=m)
+        xs = x.cpu().numpy()
+        if prec == "fp32":
+            assert torch.equal(f_out, f_sep)
+            assert _rel(fh_out.cpu().numpy(), fh_sep.cpu().numpy()) < 1e-6
+            tol = 1e-6
+        else:
+            tol = 1e-12
+        assert _rel(f_out.cpu().numpy(), o.trafo(xs, fh.cpu().numpy())[0]) < tol
+        assert _rel(fh_out.cpu().numpy(), o.adj(xs, f_in.cpu().numpy()).ravel()) < tol
+    f_sep, g_sep, _ = pg.trafo_device(xg, fhg, lib.COMPUTE_F | lib.COMPUTE_GRAD_F)
+    torch.cuda.synchronize()
+    assert torch.equal(fg, f_sep) and torch.equal(gg, g_sep)
+    ok = oracle.OraclePlan((16, 16, 16), m=6)
+    for fh, fo in rhs:
+        f_sep, _, _ = pk.trafo_device(xk, fh, lib.COMPUTE_F)
+        torch.cuda.synchronize()
+        assert torch.equal(fo, f_sep)
+        assert _rel(fo.cpu().numpy(), ok.trafo(xk.cpu().numpy(), fh.cpu().numpy())[0]) < 1e-6
+    # the captured graph of the fused batch
+    want = [(r[7].clone(), r[8].clone()) for r in ref] + [fo.clone() for _, fo in rhs]
+    batch.capture()
+    for r in ref:
+        r[7].zero_()
+        r[8].zero_()
+    for _, fo in rhs:
+        fo.zero_()
+    batch.run()
+    batch.synchronize()
+    for r, (wf, wa) in zip(ref, want):
+        assert torch.equal(r[7], wf)
+        assert _rel(r[8].cpu().numpy(), wa.cpu().numpy()) < 1e-6
+    for (_, fo), w in zip(rhs, want[len(ref):]):
+        assert torch.equal(fo, w)
