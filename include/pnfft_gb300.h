@@ -89,16 +89,18 @@ int pnfft_gb300_set_tuning(pnfft_plan ths, const int *tuning3);
 
 /* Batched convolutions (no counterpart in the reference).  Between
  * pnfft_gb300_batch_begin(stream) and pnfft_gb300_batch_end(), every
- * pnfft_trafo / pnfft_adj on that stream (pnfft_gb300_set_stream) with device
+ * pnfft_trafo / pnfft_adj (on any stream) with device
  * arrays attached, fixed nodes, an FP32-mixed plan, COMPUTE_F alone, the
  * line kernels (conv method 0; no ik, interlacing, gradient or Hessian) and
  * fewer line sub-problems than 4 CTAs per SM (a call too small to fill the
  * GPU alone; larger calls keep their grid in L2 from D to B) runs
  * its binning and D + F (trafo) or binning and grid clearing (adjoint) at
  * once, each into a grid of its own, and defers its convolution.
- * pnfft_gb300_batch_end launches, per direction and cutoff, one kernel over
- * the sub-problems of all deferred calls, then the adjoints' F^H and D^T, all
- * on the stream, without synchronizing.  Other calls run as usual.  The calls
+ * pnfft_gb300_batch_end makes the batch's stream wait for the deferred calls
+ * (an event per call) and launches there, per direction and cutoff, one
+ * kernel over the sub-problems of all deferred calls, then the adjoints' F^H
+ * and D^T, without synchronizing; the deferred outputs are ready in the
+ * batch's stream order.  Other calls run as usual.  The calls
  * of a batch must be independent: none may read an array another one writes.
  * A batch can be captured into a CUDA graph after one uncaptured run of the
  * same calls (which allocates the grids).  Returns 0 on success. */

@@ -30,11 +30,11 @@ __all__ = ["Batch"]
 class Batch:
     """streams: the number of branches the plans are spread over (all items of
     one plan stay on one branch, in the order they were added); branches run
-    concurrently, in eager runs and in the captured graph.  fused: instead of
-    branches, all items on one stream inside a pnfft_gb300 batch, so that the
-    convolutions of all calls that qualify (FP32-mixed, f alone, line kernels)
-    run as one launch per direction and cutoff; the items must be
-    independent (no item reads what another writes)."""
+    concurrently, in eager runs and in the captured graph.  fused: the
+    branches run inside a pnfft_gb300 batch, so that the convolutions of the
+    small calls that qualify (FP32-mixed, f alone, line kernels) run as one
+    launch per direction and cutoff; the items must be independent (no item
+    reads what another writes)."""
 
     def __init__(self, device=None, streams=4, fused=False):
         self.fused = bool(fused)
@@ -100,19 +100,18 @@ class Batch:
                 self.stream.wait_stream(s)
 
     def _run_fused(self):
-        """All items on the batch stream inside pnfft_gb300_batch_begin / _end:
-        the FP32-mixed f-only line convolutions of all plans run as one launch
-        per direction and cutoff."""
+        """The branches inside pnfft_gb300_batch_begin / _end on the batch
+        stream: the FP32-mixed f-only line convolutions of the calls too small
+        to fill the GPU run as one launch per direction and cutoff once the
+        branches have joined; the larger calls run on their branches."""
         L = load()
-        with torch.cuda.stream(self.stream):
-            L.pnfft_gb300_clear_error()
-            _check(L.pnfft_gb300_batch_begin(_stream_handle(self.stream)), "pnfft_gb300_batch_begin")
-            try:
-                for it in self.items:
-                    self._run_item(it)
-            finally:
-                rc = L.pnfft_gb300_batch_end()
-            _check(rc, "pnfft_gb300_batch_end")
+        L.pnfft_gb300_clear_error()
+        _check(L.pnfft_gb300_batch_begin(_stream_handle(self.stream)), "pnfft_gb300_batch_begin")
+        try:
+            self._run_branches()
+        finally:
+            rc = L.pnfft_gb300_batch_end()
+        _check(rc, "pnfft_gb300_batch_end")
 
     def fused_stats(self):
         """(calls deferred, batched convolution launches) of the last fused run."""

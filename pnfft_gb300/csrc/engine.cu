@@ -76,6 +76,7 @@ struct DevState {
   // replays
   std::vector<void *> bgrid;
   std::vector<ConvArgs *> bargs;
+  std::vector<cudaEvent_t> bev;  // recorded on the call's stream once its part before B / B^T is issued
   int bslot = 0;  // deferred calls of this plan in the open batch
 };
 
@@ -335,13 +336,14 @@ static NodeDev *node_dev(pnfft_nodes nd) {
 // batched convolutions
 //
 // Between pnfft_gb300_batch_begin(stream) and pnfft_gb300_batch_end(), a call
-// on that stream with device arrays, fixed nodes and an FP32-mixed f-only
+// (on any stream) with device arrays, fixed nodes and an FP32-mixed f-only
 // line convolution (no ik, interlacing, gradient or Hessian) too small to
 // fill the GPU alone runs its binning
 // and D + F (trafo) or its binning and grid clearing (adjoint) at once into a
-// grid of its own, and defers B or B^T.  The end of the batch launches one
-// kernel per direction and cutoff over the line sub-problems of all deferred
-// calls (up to kMultiItems per launch), then the adjoints' F^H and D^T.  The
+// grid of its own, and defers B or B^T.  The end of the batch waits on the
+// batch stream for the deferred calls (an event per call), launches one kernel
+// per direction and cutoff over the line sub-problems of all deferred calls
+// (up to kMultiItems per launch), then the adjoints' F^H and D^T.  The
 // calls of a batch must be independent (none reads what another writes).
 // ---------------------------------------------------------------------------
 struct Deferred {
@@ -350,6 +352,7 @@ struct Deferred {
   int adjoint, cut, max_subs;
   const ConvArgs *dargs;  // the call's arguments in device memory
   void *grid;
+  cudaEvent_t ev;         // the batch stream waits for it before the batched launch
   DeconvArgs da;          // adjoint: D^T after F^H on `grid`
 };
 
@@ -388,23 +391,28 @@ static bool batch_small(const Binning &b) {
 // the grid and argument slot of the plan's next deferred call; false (the
 // call then runs as usual) where a slot would need an allocation during a
 // stream capture or the allocation fails
-static bool batch_slot(pnfft_plan p, void **grid, ConvArgs **dargs) {
+static bool batch_slot(pnfft_plan p, void **grid, ConvArgs **dargs, cudaEvent_t *ev) {
   DevState *d = p->dev;
   const int k = d->bslot;
-  if (k >= (int)d->bgrid.size() || k >= (int)d->bargs.size()) {
+  if (k >= (int)d->bgrid.size()) {
     if (d->capturing) return false;
     void *g = nullptr;
     ConvArgs *a = nullptr;
-    if (cudaMalloc(&g, d->grid_bytes) != cudaSuccess || cudaMalloc(&a, sizeof(ConvArgs)) != cudaSuccess) {
+    cudaEvent_t e = nullptr;
+    if (cudaMalloc(&g, d->grid_bytes) != cudaSuccess || cudaMalloc(&a, sizeof(ConvArgs)) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
       cudaGetLastError();
       if (g) cudaFree(g);
+      if (a) cudaFree(a);
       return false;
     }
     d->bgrid.push_back(g);
     d->bargs.push_back(a);
+    d->bev.push_back(e);
   }
   *grid = d->bgrid[k];
   *dargs = d->bargs[k];
+  *ev = d->bev[k];
   if (d->bslot++ == 0) g_batch.plans.push_back(p);
   return true;
 }
@@ -413,6 +421,7 @@ static int batch_flush() {
   if (g_batch.items.empty()) return 0;
   const cudaStream_t s = g_batch.s;
   std::vector<Deferred> &items = g_batch.items;
+  for (const Deferred &it : items) PG_CUDA(cudaStreamWaitEvent(s, it.ev, 0));
   for (int adj = 0; adj < 2; adj++) {
     std::vector<int> cuts;
     for (const Deferred &it : items)
@@ -958,12 +967,14 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       // an open batch defers B: D and F go to the call's own grid
       void *bgrid = nullptr;
       ConvArgs *bdargs = nullptr;
+      cudaEvent_t bev = nullptr;
       bool defer = false;
-      if (g_batch.active && zc && fork && !il_plan && !ik && nd->fixed && s == g_batch.s && (cflags & C_F) &&
+      if (g_batch.active && zc && fork && !il_plan && !ik && nd->fixed && (cflags & C_F) &&
           !(cflags & (C_GRAD | C_HESS | PNFFT_OMIT_CONV | PNFFT_OMIT_FFT | PNFFT_OMIT_DECONV))) {
         ConvArgs probe = ca;
         probe.bin = pass_bin[0];
-        defer = interp_line_chosen(probe, 1, f32) && batch_small(probe.bin) && batch_slot(p, &bgrid, &bdargs);
+        defer = interp_line_chosen(probe, 1, f32) && batch_small(probe.bin) &&
+                batch_slot(p, &bgrid, &bdargs, &bev);
       }
       if (defer) {
         ca.grid = bgrid;
@@ -1034,6 +1045,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
             c.hess_out = A.hess;
             if (defer) {
               store_conv_args(c, bdargs, s);
+              PG_CUDA(cudaEventRecord(bev, s));
               Deferred it;
               memset(&it, 0, sizeof(it));
               it.p = p;
@@ -1043,6 +1055,7 @@ int engine_trafo(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
               it.max_subs = c.bin.max_subs;
               it.dargs = bdargs;
               it.grid = bgrid;
+              it.ev = bev;
               g_batch.items.push_back(it);
               g_batch.deferred++;
               p->last_conv[0] = CONV_LINE;
@@ -1148,12 +1161,14 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
       // an open batch defers B^T, and F^H and D^T after it, on the call's own grid
       void *bgrid = nullptr;
       ConvArgs *bdargs = nullptr;
+      cudaEvent_t bev = nullptr;
       bool defer = false;
-      if (g_batch.active && zc && fork && !il_plan && !ik && nd->fixed && s == g_batch.s && (cflags & C_F) &&
+      if (g_batch.active && zc && fork && !il_plan && !ik && nd->fixed && (cflags & C_F) &&
           !(cflags & (C_GRAD | PNFFT_OMIT_CONV | PNFFT_OMIT_FFT | PNFFT_OMIT_DECONV))) {
         ConvArgs probe = ca;
         probe.bin = pass_bin[0];
-        defer = spread_line_f_chosen(probe, 1, f32) && batch_small(probe.bin) && batch_slot(p, &bgrid, &bdargs);
+        defer = spread_line_f_chosen(probe, 1, f32) && batch_small(probe.bin) &&
+                batch_slot(p, &bgrid, &bdargs, &bev);
       }
       for (int pass = 0; pass < (il_plan ? 2 : 1); pass++) {
         const int il = il_plan ? pass : 0;
@@ -1173,9 +1188,11 @@ int engine_adj(pnfft_plan p, pnfft_nodes nd, unsigned cflags) {
             c.f_in = fin;
             c.grad_in = gin;
             store_conv_args(c, bdargs, s);
+            PG_CUDA(cudaEventRecord(bev, s));
             Deferred it;
             memset(&it, 0, sizeof(it));
             it.p = p;
+            it.ev = bev;
             it.slot = &node_dev(nd)->bins[0][0];
             it.adjoint = 1;
             it.cut = p->cutoff;
@@ -1468,6 +1485,7 @@ void engine_release_plan(pnfft_plan p) {
     cudaStreamSynchronize(d->stream);
     for (void *g : d->bgrid) cudaFree(g);  // cudaFree waits for the device
     for (ConvArgs *a : d->bargs) cudaFree(a);
+    for (cudaEvent_t e : d->bev) cudaEventDestroy(e);
     d->pending.clear();
     if (d->grid) cudaFree(d->grid);
     if (d->fft_prec >= 0) cufftDestroy(d->fft);
