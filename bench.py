@@ -302,6 +302,23 @@ def run_gpu(args):
             "frac_by_kernel": {kernels["interp"]: tflops(b_ms) / peak_ffma2.value,
                                kernels["spread"]: tflops(bt_ms) / peak_ffma2.value},
             "hbm": {"achieved": gbs, "peak": hbm, "unit": "GB/s", "frac": gbs / hbm, "peak_source": peak_kind}}
+    # the step's roofline: per stage the larger of its compulsory bytes over
+    # the measured HBM bandwidth and its flops over the measured FP32 rate,
+    # summed over one trafo + adj, against the measured step time
+    nn, NN = int(np.prod(n)), int(np.prod(N))
+    peak_f = peak_ffma2.value * 1e12
+    t_stage = {
+        "binning_x2": 2 * M * (24 + 16 + 4) / (hbm * 1e9),         # x in, records and permutation out
+        "D": (NN * 16 + nn * 8) / (hbm * 1e9),                       # f_hat in, padded grid out
+        "F_x2": 2 * (2 * 2 * nn * 8) / (hbm * 1e9),                  # two passes over the grid each way
+        "B": max(alg_bytes / (hbm * 1e9), alg_flops / peak_f),
+        "BT": max(alg_bytes / (hbm * 1e9), alg_flops / peak_f),
+        "DT": (nn * 8 + NN * 32) / (hbm * 1e9),                      # grid in, f_hat read and written
+    }
+    t_roof = sum(t_stage.values())
+    roof["step"] = {"t_roof_ms": 1e3 * t_roof, "t_measured_ms": step_ms, "frac": 1e3 * t_roof / step_ms,
+                    "stages_roof_ms": {k: 1e3 * v for k, v in t_stage.items()},
+                    "rule": "sum over stages of max(bytes / measured HBM, flops / measured FP32 FFMA2)"}
     traffic_file = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(traffic_file):
         try:
