@@ -88,24 +88,109 @@ __device__ __forceinline__ void window_row(const WindowArgs &w, bool poly, const
   }
 }
 
+// The FP32 window polynomials in pairs of stencil points, for paired FMAs:
+// for axis t and pair cp (points 2 cp and 2 cp + 1), coefficient k of both
+// points at s_pp[((t * NP + cp) * 16 + k) * 2 + {0, 1}] (zero for a point
+// beyond CUT), so that one 16-byte load gives two coefficients of the pair.
+template <int CUT>
+struct PolyPairs {
+  static constexpr int NP = (CUT + 1) / 2;
+  static constexpr int FLOATS = 3 * NP * 32;
+};
+
+template <int CUT, int NTH>
+__device__ __forceinline__ void stage_poly_pairs(const float *poly, float *s_pp, int tid) {
+  constexpr int NP = PolyPairs<CUT>::NP;
+  for (int i = tid; i < 3 * NP * 16; i += NTH) {
+    const int k = i & 15, cp = (i >> 4) % NP, t = (i >> 4) / NP;
+    const int c0 = 2 * cp, c1 = c0 + 1;
+    const float v0 = __ldg(poly + (t * CUT + c0) * kPolyCoef + k);
+    const float v1 = c1 < CUT ? __ldg(poly + (t * CUT + c1) * kPolyCoef + k) : 0.f;
+    *(float2 *)(s_pp + 2 * i) = make_float2(v0, v1);
+  }
+}
+
+// The psi row of one node on one axis as window_row, two stencil points per
+// paired FMA (each lane rounds like fmaf, in the same Horner order: the same
+// values bit for bit)
+template <int CUT>
+__device__ __forceinline__ void window_row_pp(const WindowArgs &w, bool poly, const float *s_pp, int t, float dist,
+                                              float *v) {
+  constexpr int NP = PolyPairs<CUT>::NP;
+  if (!poly) {
+#pragma unroll
+    for (int c = 0; c < CUT; c++) {
+      float out[3];
+      window_point<float>(w, t, c, dist, 0, out);
+      v[c] = out[0];
+    }
+    return;
+  }
+  const float u = dist - 0.5f;
+  const float2 u2 = make_float2(u, u);
+  const bool short_rows = w.poly_ncoef <= 12;
+#pragma unroll
+  for (int cp = 0; cp < NP; cp++) {
+    const float4 *r = (const float4 *)(s_pp + (t * NP + cp) * 32);  // r[j]: coefficients 2j, 2j + 1 of both points
+    float2 h;
+    if (short_rows) {
+      const float4 q5 = r[5];
+      h = make_float2(q5.z, q5.w);
+      h = __ffma2_rn(h, u2, make_float2(q5.x, q5.y));
+    } else {
+      const float4 q7 = r[7], q6 = r[6], q5 = r[5];
+      h = make_float2(q7.z, q7.w);
+      h = __ffma2_rn(h, u2, make_float2(q7.x, q7.y));
+      h = __ffma2_rn(h, u2, make_float2(q6.z, q6.w));
+      h = __ffma2_rn(h, u2, make_float2(q6.x, q6.y));
+      h = __ffma2_rn(h, u2, make_float2(q5.z, q5.w));
+      h = __ffma2_rn(h, u2, make_float2(q5.x, q5.y));
+    }
+#pragma unroll
+    for (int j = 4; j >= 0; j--) {
+      const float4 q = r[j];
+      h = __ffma2_rn(h, u2, make_float2(q.z, q.w));
+      h = __ffma2_rn(h, u2, make_float2(q.x, q.y));
+    }
+    v[2 * cp] = h.x;
+    if (2 * cp + 1 < CUT) v[2 * cp + 1] = h.y;
+  }
+  if (w.kind == WIN_BESSEL_I0 && dist == 0.f) {  // the fit is not used at the removable singularity
+    float out[3];
+    window_point<float>(w, t, 0, dist, 0, out);
+    v[0] = out[0];
+  }
+}
+
 // Kahan-compensated sum of the shares part[r], part[r + 4], ... (below NTH)
-// in that fixed order, returned as the compensated value (sum minus the
-// carried correction).  The four threads r = 0..3 of a node each take a
+// in a fixed order, returned as the compensated value (sum minus the carried
+// correction).  The four threads r = 0..3 of a node each take a
 // quarter of the node's shares: a plain FP32 run of NTH / 4 additions is the
 // largest rounding term of the interpolation (about two thirds of the FP32
 // error of B on uniform nodes at m = 6), compensation leaves it at the level
 // of the grid and window rounding.
 template <int NTH>
 __device__ __forceinline__ float2 kahan_quarter_sum(const float2 *part, int r) {
-  float2 s = make_float2(0.f, 0.f), c = s;
-#pragma unroll 8
-  for (int k = r; k < NTH; k += 4) {
+  // two compensated runs (shares r, r + 8, ... and r + 4, r + 12, ...) halve
+  // the length of the dependent chain
+  float2 s = make_float2(0.f, 0.f), c = s, u = s, e = s;
+#pragma unroll 4
+  for (int k = r; k < NTH; k += 8) {
     const float2 y = __fadd2_rn(part[k], make_float2(-c.x, -c.y));
     const float2 t = __fadd2_rn(s, y);
     c = __fadd2_rn(__fadd2_rn(t, make_float2(-s.x, -s.y)), make_float2(-y.x, -y.y));
     s = t;
+    const float2 y2 = __fadd2_rn(part[k + 4], make_float2(-e.x, -e.y));
+    const float2 t2 = __fadd2_rn(u, y2);
+    e = __fadd2_rn(__fadd2_rn(t2, make_float2(-u.x, -u.y)), make_float2(-y2.x, -y2.y));
+    u = t2;
   }
-  return __fadd2_rn(s, make_float2(-c.x, -c.y));
+  // s + u with its rounding error (TwoSum), then the two corrections
+  const float2 t = __fadd2_rn(s, u);
+  const float2 bb = __fadd2_rn(t, make_float2(-s.x, -s.y));
+  const float2 err = __fadd2_rn(__fadd2_rn(s, make_float2(-(t.x - bb.x), -(t.y - bb.y))),
+                                __fadd2_rn(u, make_float2(-bb.x, -bb.y)));
+  return __fadd2_rn(t, __fadd2_rn(err, make_float2(-(c.x + e.x), -(c.y + e.y))));
 }
 
 // The item and sub-problem of block `blk` of a MultiConv launch, and a copy of
