@@ -41,25 +41,6 @@ struct GradGeom32 {
   static_assert(WS % 4 == 0, "16-byte aligned node rows");
 };
 
-// one window row of CUT values: derivative `der` (0 or 1) on axis t
-template <int CUT>
-__device__ __forceinline__ void window_row_d(const WindowArgs &w, bool poly, const float *s_poly, int der, int t,
-                                             float dist, float *v) {
-  constexpr int PS = LineGeom32<CUT>::PS;
-#pragma unroll
-  for (int c = 0; c < CUT; c++) {
-    if (poly && !(w.kind == WIN_BESSEL_I0 && c == 0 && dist == 0.f)) {
-      const float4 *rw = (const float4 *)(s_poly + ((der * 3 + t) * CUT + c) * PS);
-      v[c] = w.poly_ncoef <= 12 ? poly_horner12(rw[0], rw[1], rw[2], dist - 0.5f)
-                                : poly_horner(rw[0], rw[1], rw[2], rw[3], dist - 0.5f);
-    } else {
-      float out[3];
-      window_point<float>(w, t, c, dist, der, out);
-      v[c] = out[der];
-    }
-  }
-}
-
 template <int CUT, int MODE>
 __global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 3) k_interp_line_g(ConvArgs a) {
   typedef LineGeom32<CUT> G;
@@ -70,7 +51,7 @@ __global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 3) k_interp_line_g(C
   constexpr bool DF = (MODE & 1) != 0;
   __shared__ __align__(16) float s_w[NB][WS];
   __shared__ __align__(16) float2 s_part[NO * NS][PR];
-  __shared__ __align__(16) float s_poly[2 * 3 * CUT * PS];
+  __shared__ __align__(16) float s_poly[PolyPairs<CUT, 6>::FLOATS];
   __shared__ __align__(16) float4 s_pre[NTH][4];  // prefetched next group of z values, per thread
   __shared__ float s_d[NB][3];
   __shared__ int s_o[NB], s_j[NB], s_slab[NB];
@@ -91,9 +72,8 @@ __global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 3) k_interp_line_g(C
   const bool vec = (n2 & 3) == 0;
   const WindowArgs &w = a.w;
   const bool poly = w.poly && w.intpol_order < 0;
-  if (poly)  // psi and psi' rows: the polynomial rows of derivatives 0 and 1
-    for (int i = tid; i < 2 * 3 * CUT * 4; i += NTH)
-      ((float4 *)(s_poly + (i >> 2) * PS))[i & 3] = __ldg((const float4 *)(w.poly + (i >> 2) * kPolyCoef) + (i & 3));
+  if (poly)  // psi and psi' rows in pairs of stencil points: the polynomial rows of derivatives 0 and 1
+    stage_poly_pairs<CUT, NTH, 6>(w.poly, s_poly, tid);
   const float scale = a.use_il ? 0.5f : 1.f;
   float2 *pre = (float2 *)s_pre[tid];
 
@@ -122,7 +102,7 @@ __global__ void __launch_bounds__(LineGeom32<CUT>::THREADS, 3) k_interp_line_g(C
       const int e = v / NB, i = v - e * NB, der = e / 3, t = e - 3 * der;
       if (i >= nb) continue;
       float val[CUT];
-      window_row_d<CUT>(w, poly, s_poly, der, t, s_d[i][t], val);
+      window_row_pp_d<CUT>(w, poly, s_poly, der, t, s_d[i][t], val);
       const int pk = s_o[i];
       float *row = s_w[i];
       if (t == 2) {

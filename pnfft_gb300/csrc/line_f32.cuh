@@ -89,49 +89,52 @@ __device__ __forceinline__ void window_row(const WindowArgs &w, bool poly, const
 }
 
 // The FP32 window polynomials in pairs of stencil points, for paired FMAs:
-// for axis t and pair cp (points 2 cp and 2 cp + 1), coefficient k of both
-// points at s_pp[((t * NP + cp) * 16 + k) * 2 + {0, 1}] (zero for a point
-// beyond CUT), so that one 16-byte load gives two coefficients of the pair.
-template <int CUT>
+// for polynomial row r (derivative der and axis t: r = 3 der + t) and pair
+// cp (points 2 cp and 2 cp + 1), coefficient k of both points at
+// s_pp[((r * NP + cp) * 16 + k) * 2 + {0, 1}] (zero for a point beyond CUT),
+// so that one 16-byte load gives two coefficients of the pair.
+template <int CUT, int NROWS = 3>
 struct PolyPairs {
   static constexpr int NP = (CUT + 1) / 2;
-  static constexpr int FLOATS = 3 * NP * 32;
+  static constexpr int FLOATS = NROWS * NP * 32;
 };
 
-template <int CUT, int NTH>
+template <int CUT, int NTH, int NROWS = 3>
 __device__ __forceinline__ void stage_poly_pairs(const float *poly, float *s_pp, int tid) {
   constexpr int NP = PolyPairs<CUT>::NP;
-  for (int i = tid; i < 3 * NP * 16; i += NTH) {
-    const int k = i & 15, cp = (i >> 4) % NP, t = (i >> 4) / NP;
+  for (int i = tid; i < NROWS * NP * 16; i += NTH) {
+    const int k = i & 15, cp = (i >> 4) % NP, r = (i >> 4) / NP;
     const int c0 = 2 * cp, c1 = c0 + 1;
-    const float v0 = __ldg(poly + (t * CUT + c0) * kPolyCoef + k);
-    const float v1 = c1 < CUT ? __ldg(poly + (t * CUT + c1) * kPolyCoef + k) : 0.f;
+    const float v0 = __ldg(poly + (r * CUT + c0) * kPolyCoef + k);
+    const float v1 = c1 < CUT ? __ldg(poly + (r * CUT + c1) * kPolyCoef + k) : 0.f;
     *(float2 *)(s_pp + 2 * i) = make_float2(v0, v1);
   }
 }
 
-// The psi row of one node on one axis as window_row, two stencil points per
-// paired FMA (each lane rounds like fmaf, in the same Horner order: the same
-// values bit for bit)
+// Derivative `der` of the window row of one node on axis t (CUT values) as
+// the single-row evaluation, two stencil points per paired FMA: each lane
+// rounds like fmaf, in the same Horner order, so the values are the same bit
+// for bit
 template <int CUT>
-__device__ __forceinline__ void window_row_pp(const WindowArgs &w, bool poly, const float *s_pp, int t, float dist,
-                                              float *v) {
+__device__ __forceinline__ void window_row_pp_d(const WindowArgs &w, bool poly, const float *s_pp, int der, int t,
+                                                float dist, float *v) {
   constexpr int NP = PolyPairs<CUT>::NP;
   if (!poly) {
 #pragma unroll
     for (int c = 0; c < CUT; c++) {
       float out[3];
-      window_point<float>(w, t, c, dist, 0, out);
-      v[c] = out[0];
+      window_point<float>(w, t, c, dist, der, out);
+      v[c] = out[der];
     }
     return;
   }
   const float u = dist - 0.5f;
   const float2 u2 = make_float2(u, u);
   const bool short_rows = w.poly_ncoef <= 12;
+  const int row = 3 * der + t;
 #pragma unroll
   for (int cp = 0; cp < NP; cp++) {
-    const float4 *r = (const float4 *)(s_pp + (t * NP + cp) * 32);  // r[j]: coefficients 2j, 2j + 1 of both points
+    const float4 *r = (const float4 *)(s_pp + (row * NP + cp) * 32);  // r[j]: coefficients 2j, 2j + 1 of both points
     float2 h;
     if (short_rows) {
       const float4 q5 = r[5];
@@ -157,9 +160,15 @@ __device__ __forceinline__ void window_row_pp(const WindowArgs &w, bool poly, co
   }
   if (w.kind == WIN_BESSEL_I0 && dist == 0.f) {  // the fit is not used at the removable singularity
     float out[3];
-    window_point<float>(w, t, 0, dist, 0, out);
-    v[0] = out[0];
+    window_point<float>(w, t, 0, dist, der, out);
+    v[0] = out[der];
   }
+}
+
+template <int CUT>
+__device__ __forceinline__ void window_row_pp(const WindowArgs &w, bool poly, const float *s_pp, int t, float dist,
+                                              float *v) {
+  window_row_pp_d<CUT>(w, poly, s_pp, 0, t, dist, v);
 }
 
 // Kahan-compensated sum of the shares part[r], part[r + 4], ... (below NTH)
