@@ -101,7 +101,9 @@ int pnfft_gb300_set_tuning(pnfft_plan ths, const int *tuning3);
  * kernel over the sub-problems of all deferred calls, then the adjoints' F^H
  * and D^T, without synchronizing; the deferred outputs are ready in the
  * batch's stream order.  Other calls run as usual.  The calls
- * of a batch must be independent: none may read an array another one writes.
+ * of a batch must be independent: none may read an array another one writes;
+ * their device arrays must stay allocated until pnfft_gb300_batch_end (a plan
+ * or node set that is freed first has its deferred calls run at that point).
  * A batch can be captured into a CUDA graph after one uncaptured run of the
  * same calls (which allocates the grids).  Returns 0 on success. */
 int pnfft_gb300_batch_begin(void *cuda_stream);

@@ -1510,7 +1510,12 @@ void engine_release_plan(pnfft_plan p) {
 void engine_release_nodes(pnfft_nodes nd) {
   NodeDev *v = nd->dev;
   if (!v) return;
-  cudaFree(v->x);
+  for (const Deferred &it : g_batch.items)
+    if (it.slot == &v->bins[0][0]) {
+      batch_flush();  // deferred calls read this node set's binning: they run first
+      break;
+    }
+  cudaFree(v->x);  // cudaFree waits for the device
   cudaFree(v->f);
   cudaFree(v->grad);
   cudaFree(v->hess);
