@@ -227,3 +227,31 @@ def test_float_api_exports_and_generators(lib):
         assert L.pnfftf_psi(p, 1, xv) == np.float32(L.pnfft_psi(dp, 1, float(np.float32(xv))))
     L.pnfftf_finalize.argtypes = [ctypes.c_void_p, ctypes.c_uint]
     L.pnfftf_finalize(p, lib.FREE_F_HAT)
+
+
+def test_batch_and_tuning_host_logic(lib):
+    """pnfft_gb300_batch_begin / _end and the tuning setters without a GPU:
+    a batch cannot be opened twice or closed unopened, an empty batch closes
+    with no deferred calls, and invalid tunings are refused."""
+    L = lib.load()
+    L.pnfft_gb300_clear_error()
+    assert L.pnfft_gb300_batch_end() != 0  # nothing open
+    L.pnfft_gb300_clear_error()
+    assert L.pnfft_gb300_batch_begin(None) != 0  # a stream is required
+    L.pnfft_gb300_clear_error()
+    assert L.pnfft_gb300_batch_begin(0x1) == 0
+    assert L.pnfft_gb300_batch_begin(0x1) != 0  # already open
+    L.pnfft_gb300_clear_error()
+    assert L.pnfft_gb300_batch_end() == 0
+    d, n = ctypes.c_int(-1), ctypes.c_int(-1)
+    assert L.pnfft_gb300_batch_stats(ctypes.byref(d), ctypes.byref(n)) == 0
+    assert (d.value, n.value) == (0, 0)
+    p = lib.Plan((8, 8, 8), m=3, precision="fp32")
+    assert p.tuning() == (0, 0, 512)
+    p.set_tuning((2, 0, 256))
+    assert p.tuning() == (2, 0, 256)
+    for bad in [(4, 0, 512), (0, -1, 512), (0, 0, 48), (0, 0, 8192)]:
+        with pytest.raises(lib.PnfftError):
+            p.set_tuning(bad)
+    assert p.tuning() == (2, 0, 256)
+    p.close()
