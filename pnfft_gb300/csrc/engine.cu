@@ -1286,6 +1286,8 @@ static int time_call(pnfft_plan p, pnfft_nodes nd, bool adjoint, unsigned flags,
 }
 
 int engine_autotune(pnfft_plan p, pnfft_nodes nd, unsigned trafo_flags, unsigned adj_flags, int reps) {
+  if (g_batch.active)  // its calls would be deferred, not timed
+    return set_error("pnfft_gb300_autotune: a batch is open (pnfft_gb300_batch_begin)"), -1;
   const int keep[2] = {p->conv_method[0], p->conv_method[1]}, keep_sub = p->line_sub_max;
   const int subs[3] = {256, 512, 2048};
   const int methods[2] = {0, 2};
