@@ -105,7 +105,8 @@ int pnfft_gb300_set_tuning(pnfft_plan ths, const int *tuning3);
  * their device arrays must stay allocated until pnfft_gb300_batch_end (a plan
  * or node set that is freed first has its deferred calls run at that point).
  * A batch can be captured into a CUDA graph after one uncaptured run of the
- * same calls (which allocates the grids).  Returns 0 on success. */
+ * same calls (which allocates the grids).  One batch is open at a time per
+ * process, and the calls come from one host thread.  Returns 0 on success. */
 int pnfft_gb300_batch_begin(void *cuda_stream);
 int pnfft_gb300_batch_end(void);
 /* Of the last closed batch: the calls whose convolution was deferred, and

@@ -182,3 +182,48 @@ def test_fused_batch_matches_separate_calls(lib, oracle):
         assert _rel(r[8].cpu().numpy(), wa.cpu().numpy()) < 1e-6
     for (_, fo), w in zip(rhs, want[len(ref):]):
         assert torch.equal(fo, w)
+
+
+def test_batch_rebinning_and_accumulated_adjoint(lib, oracle):
+    """Inside one pnfft_gb300 batch: a second trafo on the plan's node set with
+    new coordinates rebins the set, so the batch runs the first deferred call
+    before (two batched launches); an adjoint with COMPUTE_ACCUMULATED adds to
+    f_hat.  Results equal the separate calls (B bit for bit) and the oracle."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    if lib.device_count() == 0:
+        pytest.fail("no CUDA device visible for a -m gpu test")
+    L = lib.load()
+    rng = np.random.default_rng(62)
+    N, m, M = (16, 16, 16), 5, 3000
+    p = lib.Plan(N, m=m, precision="fp32")
+    o = oracle.OraclePlan(N, m=m)
+    x1 = torch.tensor(rng.uniform(-0.5, 0.5, (M, 3)), device="cuda")
+    x2 = torch.tensor(rng.uniform(-0.5, 0.5, (M, 3)), device="cuda")
+    fh = torch.tensor(rng.standard_normal(4096) + 1j * rng.standard_normal(4096), device="cuda")
+    fv = torch.tensor(rng.standard_normal(M) + 1j * rng.standard_normal(M), device="cuda")
+    f1 = torch.zeros(M, dtype=torch.complex128, device="cuda")
+    f2 = torch.zeros(M, dtype=torch.complex128, device="cuda")
+    acc0 = torch.tensor(rng.standard_normal(4096) + 1j * rng.standard_normal(4096), device="cuda")
+    acc = acc0.clone()
+    s = torch.cuda.Stream()
+    L.pnfft_gb300_clear_error()
+    lib._check(L.pnfft_gb300_batch_begin(s.cuda_stream or 1), "batch_begin")
+    with torch.cuda.stream(s):
+        p.trafo_device(x1, fh, lib.COMPUTE_F, f=f1, fixed_nodes=True)
+        p.trafo_device(x2, fh, lib.COMPUTE_F, f=f2, fixed_nodes=True)
+        p.adj_device(x2, fv, compute_flags=lib.COMPUTE_F | lib.COMPUTE_ACCUMULATED, f_hat=acc, fixed_nodes=True)
+    lib._check(L.pnfft_gb300_batch_end(), "batch_end")
+    s.synchronize()
+    d, n = ctypes.c_int(0), ctypes.c_int(0)
+    L.pnfft_gb300_batch_stats(ctypes.byref(d), ctypes.byref(n))
+    assert d.value == 3 and n.value == 3  # B of the first call; then B and B^T of the rest
+    g1, _, _ = p.trafo_device(x1, fh, lib.COMPUTE_F)
+    g2, _, _ = p.trafo_device(x2, fh, lib.COMPUTE_F)
+    torch.cuda.synchronize()
+    assert torch.equal(f1, g1) and torch.equal(f2, g2)
+    xs1, xs2 = x1.cpu().numpy(), x2.cpu().numpy()
+    assert _rel(f1.cpu().numpy(), o.trafo(xs1, fh.cpu().numpy())[0]) < 1e-6
+    assert _rel(f2.cpu().numpy(), o.trafo(xs2, fh.cpu().numpy())[0]) < 1e-6
+    want = acc0.cpu().numpy() + o.adj(xs2, fv.cpu().numpy()).ravel()
+    assert _rel(acc.cpu().numpy(), want) < 1e-6
