@@ -227,3 +227,38 @@ def test_batch_rebinning_and_accumulated_adjoint(lib, oracle):
     assert _rel(f2.cpu().numpy(), o.trafo(xs2, fh.cpu().numpy())[0]) < 1e-6
     want = acc0.cpu().numpy() + o.adj(xs2, fv.cpu().numpy()).ravel()
     assert _rel(acc.cpu().numpy(), want) < 1e-6
+
+
+def test_batch_more_calls_than_one_launch_holds(lib, oracle):
+    """70 right-hand sides on one node set in one batch: the deferred calls
+    of one cutoff go out in launches of at most 64 calls (two here), and every
+    result equals its separate call."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    if lib.device_count() == 0:
+        pytest.fail("no CUDA device visible for a -m gpu test")
+    L = lib.load()
+    rng = np.random.default_rng(63)
+    N, m, M, K = (8, 8, 8), 3, 700, 70
+    p = lib.Plan(N, m=m, precision="fp32")
+    x = torch.tensor(rng.uniform(-0.5, 0.5, (M, 3)), device="cuda")
+    fhs = [torch.tensor(rng.standard_normal(512) + 1j * rng.standard_normal(512), device="cuda") for _ in range(K)]
+    outs = [torch.zeros(M, dtype=torch.complex128, device="cuda") for _ in range(K)]
+    s = torch.cuda.Stream()
+    L.pnfft_gb300_clear_error()
+    lib._check(L.pnfft_gb300_batch_begin(s.cuda_stream or 1), "batch_begin")
+    with torch.cuda.stream(s):
+        for fh, fo in zip(fhs, outs):
+            p.trafo_device(x, fh, lib.COMPUTE_F, f=fo, fixed_nodes=True)
+    lib._check(L.pnfft_gb300_batch_end(), "batch_end")
+    s.synchronize()
+    d, n = ctypes.c_int(0), ctypes.c_int(0)
+    L.pnfft_gb300_batch_stats(ctypes.byref(d), ctypes.byref(n))
+    assert d.value == K and n.value == 2
+    o = oracle.OraclePlan(N, m=m)
+    xs = x.cpu().numpy()
+    for k in (0, 63, 64, 69):
+        g, _, _ = p.trafo_device(x, fhs[k], lib.COMPUTE_F)
+        torch.cuda.synchronize()
+        assert torch.equal(outs[k], g)
+        assert _rel(outs[k].cpu().numpy(), o.trafo(xs, fhs[k].cpu().numpy())[0]) < 1e-6
