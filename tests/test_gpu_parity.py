@@ -1,7 +1,7 @@
 """Parity of the CUDA path (through the C ABI) with the CPU oracle.
 
 FP64: every transform variant agrees with the oracle's restatement of the
-reference on the same inputs to 1e-12 relative l2 (spec bar); node
+reference on the same inputs to 1e-12 relative l2 (the FP64 bar); node
 indices and the PNFFT_SORT_NODES permutation are bit-exact.
 FP32-mixed: within 1e-6 relative l2 of the FP64 NDFT at m = 6 (FP32_TOL, the
 bar of the FP32-mixed form for f, grad_f and the adjoint); Hessians, which
