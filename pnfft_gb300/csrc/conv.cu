@@ -63,9 +63,19 @@ __global__ void k_bin_keys(const double *__restrict__ x, int64_t M, int n0, int 
       long long fnx;
       float fr;
       nx_exact(x[3 * j + d], nn[d], &fnx, &fr);
-      long long w = (fnx - m) % nn[d];
-      if (w < 0) w += nn[d];
-      u[d] = (int)w;
+      // (fnx - m) mod n: one add or subtract for the usual nodes (|n x| < n),
+      // the 64-bit remainder otherwise
+      long long w = fnx - m;
+      if (w >= -nn[d] && w < 2LL * nn[d]) {
+        int wi = (int)w;
+        wi += wi < 0 ? nn[d] : 0;
+        wi -= wi >= nn[d] ? nn[d] : 0;
+        u[d] = wi;
+      } else {
+        w %= nn[d];
+        if (w < 0) w += nn[d];
+        u[d] = (int)w;
+      }
       dist[d] = (T)fr;
     } else {
       AxisPos p = axis_pos(x[3 * j + d], nn[d], m, il);
