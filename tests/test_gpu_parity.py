@@ -240,6 +240,26 @@ def test_fp32_tiny_and_edge_coordinates(gpu, oracle):
     assert rel(p.adj(x, f), o.adj(x, f)) < FP32_TOL
 
 
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-10), ("fp32", FP32_TOL)])
+def test_coordinates_outside_the_unit_cell(gpu, oracle, prec, tol):
+    # the transform is periodic: nodes shifted by whole periods (up to 1e4,
+    # where the grid index leaves the one-period range of the wrap and takes
+    # the general remainder) give the results of the same nodes in
+    # [-0.5, 0.5); the tolerance covers the rounding of x + k in FP64
+    N = (16, 16, 16)
+    rng = np.random.default_rng(35)
+    x0 = rng.uniform(-0.5, 0.5, (1200, 3))
+    k = rng.choice(np.array([-10000, -7, -2, -1, 0, 1, 2, 3, 9999]), size=x0.shape)
+    x = x0 + k
+    xw = x - np.floor(x + 0.5)  # the same points wrapped, after the rounding of x0 + k
+    fh = rng.standard_normal(4096) + 1j * rng.standard_normal(4096)
+    f = rng.standard_normal(x.shape[0]) + 1j * rng.standard_normal(x.shape[0])
+    p = gpu.Plan(N, m=5, precision=prec)
+    o = oracle.OraclePlan(N, m=5)
+    assert rel(p.trafo(x, fh)[0], o.trafo(xw, fh)[0]) < tol
+    assert rel(p.adj(x, f), o.adj(xw, f)) < tol
+
+
 @pytest.mark.parametrize("win", list(WINDOWS))
 def test_fp32_mixed_all_windows_vs_fp64_oracle(gpu, oracle, win):
     # the FP32 windows are evaluated with a compensated argument; against the
