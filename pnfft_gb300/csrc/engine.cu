@@ -449,11 +449,21 @@ static int batch_flush() {
   for (const Deferred &it : items) {
     if (!it.adjoint) continue;
     DevState *d = it.p->dev;
+    // the plan's FFT (and its work area) on the batch stream: after the work
+    // already on the plan's stream, and before what follows there
+    if (d->stream != s) {
+      PG_CUDA(cudaEventRecord(d->ev_fork, d->stream));
+      PG_CUDA(cudaStreamWaitEvent(s, d->ev_fork, 0));
+    }
     PG_FFT(cufftSetStream(d->fft, s));
     const int rc = fft_exec_on(it.p, it.grid, CUFFT_INVERSE);
     PG_FFT(cufftSetStream(d->fft, d->stream));
     if (rc) return -1;
     launch_deconv_crop_acc(it.da, fp32(it.p), s);
+    if (d->stream != s) {
+      PG_CUDA(cudaEventRecord(d->ev_join, s));
+      PG_CUDA(cudaStreamWaitEvent(d->stream, d->ev_join, 0));
+    }
   }
   PG_CUDA(cudaGetLastError());
   for (pnfft_plan p : g_batch.plans)
