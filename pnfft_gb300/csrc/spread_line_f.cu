@@ -19,8 +19,10 @@ namespace pg {
 // exact zeros).  When a node lies in a later slab, every group of 4 slots
 // whose z leaves the window is final for this CTA: it is committed to the
 // grid with vector atomics (all-zero pairs are skipped) and cleared for the
-// z it takes next -- no register moves.  A complete commit after kFlushLineNodes
-// nodes without a slide bounds the FP32 summation length in dense clusters.
+// z it takes next -- no register moves.  A complete commit at the start of a
+// batch once kFlushLineNodes or more nodes ran without a slide bounds the FP32
+// summation length in dense clusters (at most NB + kFlushLineNodes - 1 = 127
+// nodes per run).
 // Per batch of NB nodes one thread per (axis, node) evaluates the node's
 // CUT window values on that axis and writes the node's rows: the z row, the
 // x row times f (complex) over the region's rows, and the y row over the

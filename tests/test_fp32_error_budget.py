@@ -9,7 +9,8 @@ in numpy, the summation order of the FP32-mixed line kernels:
   of a node summed by four threads, each two Kahan-compensated runs over 16
   shares combined with TwoSum, and two pairwise steps;
 - B^T (k_spread_line_f): per line of 4x4 columns, nodes in slab order, each
-  grid value accumulated in FP32 over at most 64 nodes before it is added
+  grid value accumulated in FP32 over runs of at most 127 nodes (a slab
+  change, or a batch start after 64 nodes, ends a run) before it is added
   (the float atomics) into the FP32 grid, without compensation.
 Each FP32-mixed result is compared with (a) the same FP32 terms summed in FP64
 (exact accumulation) and (b) the all-FP64 computation.  The accumulation
@@ -20,7 +21,7 @@ Asserted: for B the compensated node sums cut the total error by more than
 accumulation error (the z chains and products) at the level of the rounding
 error (below 1.5 times it); for B^T on a dense cluster the
 total stays below 1e-6 and the accumulation error (the larger part there,
-about 3e-7) below 4e-7.  The printout gives the numbers.
+3.5e-7) below 4e-7.  The printout gives the numbers.
 """
 import numpy as np
 
@@ -149,13 +150,22 @@ def spread_emulated(x, f):
     g64 = np.zeros(n ** 3, np.complex128)
     s = np.arange(CUT)
     run = np.zeros(n ** 3, np.complex64)
-    count, cur = 0, None
+    # the kernel's rule: per line (sub-problems of 512 nodes), batches of 64
+    # nodes; a slab change commits; at a batch start, 64 or more nodes since
+    # the last commit commit everything (runs of at most 127 nodes)
+    since, cur, pos, slab = 0, None, 0, None
     for j in order:
-        if cur is not None and (line[j] != cur or count == 64):
+        s_j = u[j, 2] // 4
+        new_line = cur is None or line[j] != cur or pos == 512
+        if new_line:
+            pos = 0
+        if cur is not None and (new_line or s_j != slab or (pos % 64 == 0 and since >= 64)):
             g32 = (g32 + run).astype(np.complex64)
             run[:] = 0
-            count = 0
-        cur = line[j]
+            since = 0
+        cur, slab = line[j], s_j
+        pos += 1
+        since += 1
         i0, i1, i2 = [(u[j, t] + s) % n for t in range(3)]
         idx = ((i0[:, None, None] * n + i1[None, :, None]) * n + i2[None, None, :]).ravel()
         wxy = (w32[j, 0][:, None] * w32[j, 1][None, :]).astype(np.float32)
@@ -164,7 +174,6 @@ def spread_emulated(x, f):
         np.add.at(run, idx, term)
         gex[idx] += term.astype(np.complex128)
         g64[idx] += (w64[j, 0][:, None, None] * w64[j, 1][None, :, None] * w64[j, 2][None, None, :]).ravel() * f[j]
-        count += 1
     g32 = (g32 + run).astype(np.complex64)
     return g32, gex, g64
 
