@@ -340,6 +340,20 @@ def run_gpu(args):
     k64 = max(1, min(3, args.steps))
     ms64, _, f64_out, fh64_out = device_steps(pd, k64, 1)
     err_adj = (torch.linalg.vector_norm(fh32_out - fh64_out) / torch.linalg.vector_norm(fh64_out)).item()
+    # the adjoint against the FP64 NDFT at 4096 random frequencies over all M
+    # nodes, f_hat_k = sum_j f_j exp(+2 pi i k x_j) (torch FP64 on the GPU, a
+    # check outside any timed region), beside the FP64 NFFT's own error there
+    kidx = torch.tensor(np.random.default_rng(11).choice(int(np.prod(N)), 4096, replace=False), device=dev)
+    kvec = torch.stack([kidx // (N[1] * N[2]) - N[0] // 2, (kidx // N[2]) % N[1] - N[1] // 2,
+                        kidx % N[2] - N[2] // 2], 1).to(torch.float64)
+    ndft = torch.zeros(4096, dtype=torch.complex128, device=dev)
+    for c0 in range(0, 4096, 16):
+        for j0 in range(0, M, 1 << 20):
+            ph = (2 * np.pi) * (xd[j0:j0 + (1 << 20)] @ kvec[c0:c0 + 16].T)
+            ndft[c0:c0 + 16] += (fd[j0:j0 + (1 << 20), None] * torch.polar(torch.ones_like(ph), ph)).sum(0)
+    nn_ = torch.linalg.vector_norm(ndft)
+    err_adj_ndft = (torch.linalg.vector_norm(fh32_out[kidx] - ndft) / nn_).item()
+    err_adj_ndft64 = (torch.linalg.vector_norm(fh64_out[kidx] - ndft) / nn_).item()
     err_trafo_64 = (torch.linalg.vector_norm(f64_out[:sub] - fd_direct) / torch.linalg.vector_norm(fd_direct)).item()
     value64 = M / (statistics.mean(ms64) * 1e-3) / 1e6
     pd.close()
@@ -421,7 +435,9 @@ def run_gpu(args):
             "clocks": clocks, "roofline": roof,
             "fp64": {"value": value64, "unit": "Mpts/s", "ms_per_step": statistics.mean(ms64),
                      "err_trafo_vs_ndft": err_trafo_64},
-            "accuracy": {"fp32_trafo_rel_l2_vs_fp64_ndft_4096": err_trafo, "fp32_adj_rel_l2_vs_fp64_path": err_adj},
+            "accuracy": {"fp32_trafo_rel_l2_vs_fp64_ndft_4096": err_trafo, "fp32_adj_rel_l2_vs_fp64_path": err_adj,
+                         "fp32_adj_rel_l2_vs_fp64_ndft_4096_freqs_all_nodes": err_adj_ndft,
+                         "fp64_nfft_adj_rel_l2_vs_fp64_ndft_4096_freqs_all_nodes": err_adj_ndft64},
             "amortised_fixed_nodes": {"value": M / (statistics.mean(ms_fixed) * 1e-3) / 1e6,
                                       "ms_per_step": statistics.mean(ms_fixed)},
             "with_grad": {"value": M / (statistics.mean(ms_grad) * 1e-3) / 1e6,
