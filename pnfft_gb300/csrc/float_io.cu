@@ -25,6 +25,7 @@ struct FloatDev {
   FloatBuf b[4];  // nodes: x, f, grad, hess; plan: f_hat in b[0]
   cudaStream_t stream = nullptr;
   const float *last_x = nullptr;  // nodes: the float x uploaded last
+  uint64_t x_ver = 0;             // nodes: the node version of that upload (0: none)
 };
 
 void float_dev_free(FloatDev *d) {
@@ -117,9 +118,15 @@ bool begin(pnfftf_plan ths, pnfftf_nodes nodes, cudaStream_t *s) {
     return false;
   }
   // a new x array means new coordinates (as pnfft_set_x of the double API)
-  if (nodes->dev->last_x != nodes->x) nodes->nd->version++;
-  nodes->dev->last_x = nodes->x;
-  return upload(nodes->dev->b[0], nodes->x, 3 * M, *s);
+  FloatDev *v = nodes->dev;
+  if (v->last_x != nodes->x) nodes->nd->version++;
+  v->last_x = nodes->x;
+  // fixed nodes (pnfftf_precompute_psi): the device copy of x is reused, as
+  // the double API does with host arrays
+  if (nodes->nd->fixed && v->x_ver == nodes->nd->version && v->b[0].cap >= 3 * M) return true;
+  if (!upload(v->b[0], nodes->x, 3 * M, *s)) return false;
+  v->x_ver = nodes->nd->version;
+  return true;
 }
 
 bool finish(pnfftf_plan ths) {
