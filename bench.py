@@ -11,7 +11,20 @@ data).  One step = pnfft_trafo (D, F, B) + pnfft_adj (B^T, F^H, D^T).
   e2e     same metric through the C ABI (pnfft_trafo/pnfft_adj) on host
           arrays from pnfft_malloc (page-locked): copies inside the timed step
   fp64    the plain FP64 path, same workload
+  roofline  the dominant kernel against the FP32 FFMA2 rate measured in the
+          run, its ncu DRAM traffic (profiles/traffic.json), and the whole
+          step's roofline (sum of stage roofline times / step time)
+  accuracy  FP32-mixed trafo against the FP64 NDFT on 4096 nodes, adjoint
+          against the FP64 NDFT at 4096 frequencies over all nodes
+  cpu_baseline  the oracle (FP64 restatement of the reference, all host
+          cores) on whole steps of the same workload
+Further rows (one GPU): with_grad, pre_cub_psi, amortised_fixed_nodes,
+batched (65 plans + 8 right-hand sides in one CUDA graph), particles
+(clustered c2r charges, autotuned), charge_dipole (one C call against four),
+float_api (pnfftf_* on host float arrays).  --impl reference times the oracle
+alone on whole steps (the reference arm).
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+       [--no-cpu] [--no-batch] [--profile]
 """
 import argparse
 import ctypes
