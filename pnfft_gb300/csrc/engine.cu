@@ -62,7 +62,8 @@ struct DevState {
   int fft_prec = -1;
   double *inv[3] = {nullptr, nullptr, nullptr};
   void *tab[3][3] = {{nullptr}};
-  float *poly = nullptr;  // fitted FP32 window polynomials (nullptr: use the formula)
+  float *poly = nullptr;  // fitted FP32 window polynomials (nullptr: use the formula), then their pairs
+  size_t poly_rows = 0;   // floats of the rows (the pairs follow)
   int poly_ncoef = kPolyCoef;  // coefficients used of each row (12 or 16)
   uint64_t tables_for = ~0ull;
   double *fhat = nullptr;
@@ -301,6 +302,16 @@ static int ensure_tables(pnfft_plan p) {
     std::vector<float> h;
     for (int nc : {12, kPolyCoef}) {
       if (fit_window_poly(p, h, nc)) {
+        // the rows, then the same coefficients in pairs of stencil points
+        const int cut = p->cutoff, np = (cut + 1) / 2;
+        d->poly_rows = h.size();
+        h.resize(d->poly_rows + (size_t)9 * np * 32, 0.f);
+        float *pp = h.data() + d->poly_rows;
+        for (int r = 0; r < 9; r++)
+          for (int cp = 0; cp < np; cp++)
+            for (int k = 0; k < kPolyCoef; k++)
+              for (int l = 0; l < 2; l++)
+                if (2 * cp + l < cut) pp[((r * np + cp) * 16 + k) * 2 + l] = h[(size_t)(r * cut + 2 * cp + l) * kPolyCoef + k];
         PG_CUDA(cudaMalloc(&d->poly, sizeof(float) * h.size()));
         PG_CUDA(cudaMemcpy(d->poly, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice));
         d->poly_ncoef = nc;
@@ -690,6 +701,7 @@ static WindowArgs window_args(pnfft_plan p) {
     for (int t = 0; t < 3; t++) w.tab[der][t] = p->dev->tab[der][t];
   w.poly = p->dev->poly;
   w.poly_ncoef = p->dev->poly_ncoef;
+  w.poly_pp = p->dev->poly ? p->dev->poly + p->dev->poly_rows : nullptr;
   return w;
 }
 

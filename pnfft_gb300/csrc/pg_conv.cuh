@@ -175,6 +175,41 @@ __device__ __forceinline__ float poly_eval(const float *row, float u, int ncoef)
   return poly_horner(__ldg(r), __ldg(r + 1), __ldg(r + 2), __ldg(r + 3), u);
 }
 
+// psi (and derivatives up to nder) of stencil points 2 cp and 2 cp + 1 on
+// axis t from the paired polynomial rows (FP32-mixed plans with fitted
+// polynomials), two points per paired FMA: each lane rounds like fmaf, in the
+// Horner order of poly_eval, so the values equal window_point's bit for bit
+// (except the Bessel-I0 point that window_point evaluates by the formula)
+__device__ __forceinline__ void window_pair(const WindowArgs &w, int t, int cp, float dist, int nder, float2 *out) {
+  const int np = (w.cut + 1) / 2;
+  const float u = dist - 0.5f;
+  const float2 u2 = make_float2(u, u);
+  for (int d = 0; d <= nder; d++) {
+    const float4 *r = (const float4 *)(w.poly_pp + ((d * 3 + t) * np + cp) * 32);  // r[j]: coefficients 2j, 2j + 1
+    float2 h;
+    if (w.poly_ncoef <= 12) {
+      const float4 q5 = __ldg(r + 5);
+      h = make_float2(q5.z, q5.w);
+      h = __ffma2_rn(h, u2, make_float2(q5.x, q5.y));
+    } else {
+      const float4 q7 = __ldg(r + 7), q6 = __ldg(r + 6), q5 = __ldg(r + 5);
+      h = make_float2(q7.z, q7.w);
+      h = __ffma2_rn(h, u2, make_float2(q7.x, q7.y));
+      h = __ffma2_rn(h, u2, make_float2(q6.z, q6.w));
+      h = __ffma2_rn(h, u2, make_float2(q6.x, q6.y));
+      h = __ffma2_rn(h, u2, make_float2(q5.z, q5.w));
+      h = __ffma2_rn(h, u2, make_float2(q5.x, q5.y));
+    }
+#pragma unroll
+    for (int j = 4; j >= 0; j--) {
+      const float4 q = __ldg(r + j);
+      h = __ffma2_rn(h, u2, make_float2(q.z, q.w));
+      h = __ffma2_rn(h, u2, make_float2(q.x, q.y));
+    }
+    out[d] = h;
+  }
+}
+
 // psi (and derivatives up to nder) of stencil point s on axis t for a node at
 // fractional position dist, from the interpolation table, the fitted
 // polynomial (FP32) or the formula

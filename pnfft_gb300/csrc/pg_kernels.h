@@ -25,6 +25,10 @@ struct WindowArgs {
   // coefficients used, the rest zero
   const float *poly;
   int poly_ncoef;
+  // the same polynomials in pairs of stencil points (points 2cp and 2cp + 1,
+  // zero beyond the cutoff): row r = 3 der + axis, coefficient k of both at
+  // poly_pp[((r * NP + cp) * 16 + k) * 2 + {0, 1}], NP = (cut + 1) / 2
+  const float *poly_pp;
 };
 constexpr int kPolyCoef = 16;
 

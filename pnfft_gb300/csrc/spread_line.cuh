@@ -208,13 +208,8 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? ((MOD
     // --- window values: all threads over (node, axis, stencil point) ------------
     // node-fastest (broadcast polynomial rows); the odd row stride in 16-byte
     // units keeps these stores to at most 4-way bank conflicts
-#pragma unroll 4  // independent polynomial chains per thread
-    for (int v = tid; v < NB * 3 * CUT; v += nth) {
-      const int e = v / NB, i = v - e * NB;
-      if (i >= nb) continue;
-      const int t = e / CUT, sidx = e - t * CUT;
-      T out[3];
-      window_point<T>(a.w, t, sidx, s_d[i][t], NDER, out);
+    // one stencil point's window values into the node's row
+    auto put = [&](int i, int t, int sidx, const T *out) {
       if (FONLY) {
         const int pk = s_o[i];
         if (t == 2) {
@@ -231,6 +226,42 @@ __global__ void __launch_bounds__(LineGeom<CUT>::THREADS, sizeof(T) == 4 ? ((MOD
         const int pos = (t == 2) ? ((s_o[i] >> 16) & (TL - 1)) + sidx : WP + t * CP + sidx;
         s_w[i][pos] = out[0];
         s_w[i][WREC + pos] = out[1];
+      }
+    };
+    bool paired = false;
+    if constexpr (sizeof(T) == 4) {
+      // fitted FP32 polynomials: two stencil points per paired FMA
+      if (a.w.poly_pp && a.w.intpol_order < 0) {
+        paired = true;
+        constexpr int NP = (CUT + 1) / 2;
+        for (int v = tid; v < NB * 3 * NP; v += nth) {
+          const int e2 = v / NB, i = v - e2 * NB;
+          if (i >= nb) continue;
+          const int t = e2 / NP, cp = e2 - t * NP;
+          const float dist = s_d[i][t];
+          float2 h[2];
+          window_pair(a.w, t, cp, dist, NDER, h);
+          T o0[2] = {h[0].x, NDER ? h[1].x : 0.f}, o1[2] = {h[0].y, NDER ? h[1].y : 0.f};
+          if (a.w.kind == WIN_BESSEL_I0 && cp == 0 && dist == 0.f) {  // evaluated by the formula there
+            T out[3];
+            window_point<T>(a.w, t, 0, dist, NDER, out);
+            o0[0] = out[0];
+            if (NDER) o0[1] = out[1];
+          }
+          put(i, t, 2 * cp, o0);
+          if (2 * cp + 1 < CUT) put(i, t, 2 * cp + 1, o1);
+        }
+      }
+    }
+    if (!paired) {
+#pragma unroll 4  // independent polynomial chains per thread
+      for (int v = tid; v < NB * 3 * CUT; v += nth) {
+        const int e = v / NB, i = v - e * NB;
+        if (i >= nb) continue;
+        const int t = e / CUT, sidx = e - t * CUT;
+        T out[3];
+        window_point<T>(a.w, t, sidx, s_d[i][t], NDER, out);
+        put(i, t, sidx, out);
       }
     }
     __syncthreads();
